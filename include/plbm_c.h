@@ -1,0 +1,150 @@
+/*
+ * plbm_c.h — C ABI of portlbm_gb300, the GB300 (sm_103a) implementation of PortLBM's
+ * per-timestep D2Q9 BGK update.
+ *
+ * Each entry point replaces one member of the reference's public API
+ * (SC-SGS/PortLBM, paths relative to that project):
+ *   lbm::create_handler(const core::Properties&)      include/lbm/portlbm_factory.hpp:59
+ *   lbm::create_handler(const std::string& settings)  include/lbm/portlbm_factory.hpp:73
+ *   execution::AlgorithmHandler virtual API           include/lbm/execution/algorithm_handler.hpp:40-156
+ * The C++ wrapper in portlbm_gb300.hpp maps these calls back to that class API and the
+ * status codes back to the reference's exception types.
+ *
+ * All functions return PLBM_OK (0) or a negative status; plbm_last_error() then holds
+ * the message.  Handles are not thread-safe except as documented for start/pause.
+ * Plain pointers and sizes only: no C++ or torch types cross this boundary.
+ */
+#ifndef PLBM_C_H
+#define PLBM_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  PROPERTY  <-> lbm::exceptions::json::PropertyArgumentException
+ *                UNKNOWN   <-> lbm::exceptions::Exception ("Unknown algorithm/data layout")
+ *                WAIT      <-> lbm::exceptions::algorithm::WaitException
+ *                IO/PARSE  <-> nlohmann::json parse or missing-key errors of json_to_properties */
+enum {
+    PLBM_OK = 0,
+    PLBM_ERR_PROPERTY = -1,
+    PLBM_ERR_UNKNOWN = -2,
+    PLBM_ERR_WAIT = -3,
+    PLBM_ERR_CUDA = -4,
+    PLBM_ERR_IO = -5,
+    PLBM_ERR_PARSE = -6,
+    PLBM_ERR_ARGUMENT = -7,
+    PLBM_ERR_NUMERIC = -8,
+    PLBM_ERR_NO_DEVICE = -9
+};
+
+/* Which result array plbm_get_results() returns (core::Results, include/lbm/core/simulation.hpp:144-216). */
+enum { PLBM_DENSITY = 0, PLBM_X_VELOCITY = 1, PLBM_Y_VELOCITY = 2, PLBM_ABS_VELOCITY = 3 };
+
+/* Arithmetic form of the step.  F64_STRICT is the drop-in: IEEE double in the reference's
+ * operation order, no fused multiply-add, identical results.  F64_FAST reassociates the BGK
+ * update into fewer FP64 instructions (FMA) and agrees to <= 1e-12.  F32_REF restates the
+ * reference's USE_FLOAT build (include/lbm/core/constants.hpp:17-21).  F32, F16S and BF16S
+ * store populations in float / half / bfloat16 (the latter two shifted by w_i * rho0) and
+ * collide in FP32. */
+enum { PLBM_F64_STRICT = 0, PLBM_F64_FAST = 1, PLBM_F32_REF = 2, PLBM_F32 = 3, PLBM_F16S = 4, PLBM_BF16S = 5 };
+
+typedef struct plbm_handler plbm_handler;
+
+/* POD mirror of core::Properties (include/lbm/core/properties.hpp:30-166) as passed to its
+ * constructor (src/lbm/core/simulation.cpp:21-58): vertical/horizontal_nodes are INNER
+ * extents; the library adds the two ghost layers.  Strings are NUL-terminated and copied. */
+typedef struct {
+    const char *algorithm;      /* "nptl" | "lptl" | "npol" | "nsol" */
+    const char *data_layout;    /* "collision" | "stream" | "bundle" */
+    int debug_mode;
+    unsigned work_group_size;
+    unsigned time_steps;
+    unsigned frame_update_interval;
+    const char *scenario;       /* the reference's eight scenarios */
+    unsigned vertical_nodes;
+    unsigned horizontal_nodes;
+    double inlet_velocity_x, inlet_velocity_y, inlet_density;
+    double outlet_velocity_x, outlet_velocity_y, outlet_density;
+    double relaxation_time;
+} plbm_properties;
+
+/* Options with no counterpart in the reference; plbm_default_options() gives the drop-in. */
+typedef struct {
+    int precision;          /* PLBM_F64_STRICT ... PLBM_BF16S */
+    int nan_protection;     /* WITH_NAN_PROTECTION (CMakeLists.txt:28, default ON) */
+    int use_graph;          /* capture chunks of steps in a CUDA graph */
+    int device;             /* CUDA device ordinal */
+    const int8_t *mask;     /* optional geometry: inner W*H flags (0 fluid, 1 solid), row-major
+                               from (x=1, y=1); replaces walls + scenario stencil. Copied. */
+} plbm_options;
+
+void plbm_default_options(plbm_options *opt);
+
+/* Validates like core::Properties::validate() (src/lbm/core/simulation.cpp:60-125) without
+ * touching a GPU. */
+int plbm_validate(const plbm_properties *props);
+
+/* lbm::create_handler(props) — builds the simulation and initialises the domain on the GPU. */
+int plbm_create(const plbm_properties *props, const plbm_options *opt, plbm_handler **out);
+/* lbm::create_handler(settings_path) — reads settings.json (README.md:99-121 schema); an
+ * optional "gb300" object may carry {"precision": "f64_fast", "nanProtection": true}. */
+int plbm_create_from_json(const char *settings_path, const plbm_options *opt, plbm_handler **out);
+void plbm_destroy(plbm_handler *h);
+
+/* AlgorithmHandler::initialize()  :55-60  — rebuild; re-reads settings.json when created from one. */
+int plbm_initialize(plbm_handler *h);
+/* AlgorithmHandler::start()  — runs the remaining steps on a worker thread and returns. */
+int plbm_start(plbm_handler *h);
+/* AlgorithmHandler::pause()  — the step in flight completes, then the loop stops. */
+int plbm_pause(plbm_handler *h);
+/* AlgorithmHandler::block_until_finished()  — joins; PLBM_ERR_WAIT if never started. */
+int plbm_block_until_finished(plbm_handler *h);
+int plbm_is_finished(plbm_handler *h, int *finished);
+
+/* AlgorithmHandler::get_densities() / get_x_velocities() / get_y_velocities() /
+ * get_absolute_velocities(): host arrays of (W*H) doubles, row-major over the inner domain,
+ * owned by the handle and valid until initialize()/destroy.  Updated on frame steps
+ * (iteration % frame_update_interval == interval - 1) and when the run finishes. */
+int plbm_get_results(plbm_handler *h, int which, const double **data, size_t *count);
+
+/* get_horizontal_nodes()/get_vertical_nodes() return stored extents (inner + 2), as the
+ * reference's do; the Domain fields are core::Domain's (include/lbm/core/domain.hpp:29-85). */
+int plbm_get_extents(plbm_handler *h, unsigned *horizontal_nodes, unsigned *vertical_nodes);
+int plbm_get_domain(plbm_handler *h, unsigned out7[7]);
+int plbm_get_progress(plbm_handler *h, double *progress);
+int plbm_get_last_frametime(plbm_handler *h, double *ms);
+int plbm_get_current_iteration(plbm_handler *h, unsigned *iteration);
+int plbm_get_properties(plbm_handler *h, plbm_properties *out); /* strings owned by the handle */
+
+/* Writes settings.json like file_interaction::properties_to_json (file_interaction.cpp:11-37). */
+int plbm_properties_to_json(const plbm_properties *props, const char *path);
+/* Reads settings.json like file_interaction::json_to_properties (file_interaction.cpp:39-69);
+ * strings are copied into thread-local storage valid until the next call on this thread. */
+int plbm_json_to_properties(const char *path, int offset, plbm_properties *out);
+
+/* ---- measurement hooks (no counterpart in the reference) ------------------------------ */
+
+/* Runs n steps synchronously on the calling thread with device-resident data; writes the
+ * average device time per step (CUDA events) to *ms_per_step when non-NULL. */
+int plbm_run_steps(plbm_handler *h, unsigned n, double *ms_per_step);
+/* Copies the device results to the host arrays now (as a frame step would). */
+int plbm_sync_results(plbm_handler *h);
+/* Kernel launches issued per step (for launch accounting). */
+int plbm_launches_per_step(plbm_handler *h, unsigned *n);
+/* Algorithmic HBM bytes per node update of the hot kernel (9 loads + 9 stores). */
+int plbm_bytes_per_node(plbm_handler *h, double *bytes);
+/* Reads back the total fluid mass and momentum (FP64 reductions on the GPU). */
+int plbm_mass_momentum(plbm_handler *h, double out3[3]);
+
+/* Last error message for h (or of the last failed create when h is NULL). */
+const char *plbm_last_error(const plbm_handler *h);
+const char *plbm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,381 @@
+"""portlbm_gb300 — PortLBM's per-timestep D2Q9 BGK update on one GB300 (sm_103a).
+
+Python mirror of the reference's public API (SC-SGS/PortLBM):
+
+* ``Properties``            core::Properties (include/lbm/core/properties.hpp:30-166): the
+                            constructor takes INNER extents and stores inner + 2, like
+                            src/lbm/core/simulation.cpp:21-58; ``validate()`` raises
+                            ``PropertyArgumentException`` with the reference's messages.
+* ``create_handler``        lbm::create_handler (include/lbm/portlbm_factory.hpp:59,73), from a
+                            ``Properties`` or a settings.json path.
+* ``AlgorithmHandler``      execution::AlgorithmHandler (include/lbm/execution/
+                            algorithm_handler.hpp:40-156): initialize/start/pause/
+                            block_until_finished/is_finished and the result getters.
+
+Everything runs in ``libplbm.so`` (hand-written CUDA + C++ host code) through the C ABI of
+``include/plbm_c.h``; there is no CPU fallback.  If the library is missing or no GPU is
+present, creating a handler raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = [
+    "Properties", "create_handler", "AlgorithmHandler", "Exception", "PropertyArgumentException",
+    "WaitException", "CudaException", "ParseException", "NoDeviceException", "PRECISIONS",
+    "properties_to_json", "json_to_properties", "library_path", "load_library",
+]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+PRECISIONS = {"f64_strict": 0, "f64_fast": 1, "f32_ref": 2, "f32": 3, "f16s": 4, "bf16s": 5}
+BYTES_PER_VALUE = {0: 8, 1: 8, 2: 4, 3: 4, 4: 2, 5: 2}
+
+
+class Exception(RuntimeError):  # noqa: A001 - mirrors lbm::exceptions::Exception
+    """lbm::exceptions::Exception (include/lbm/exceptions/exceptions.hpp:31)."""
+
+
+class PropertyArgumentException(Exception):
+    """lbm::exceptions::json::PropertyArgumentException (exceptions.hpp:70)."""
+
+
+class WaitException(Exception):
+    """lbm::exceptions::algorithm::WaitException (exceptions.hpp:150)."""
+
+
+class CudaException(Exception):
+    """A CUDA runtime error inside libplbm."""
+
+
+class ParseException(Exception):
+    """settings.json could not be read or parsed (nlohmann::json errors in the reference)."""
+
+
+class NoDeviceException(CudaException):
+    """No CUDA device is visible."""
+
+
+_CODES = {-1: PropertyArgumentException, -2: Exception, -3: WaitException, -4: CudaException,
+          -5: ParseException, -6: ParseException, -7: Exception, -8: Exception, -9: NoDeviceException}
+
+
+class _CProps(ctypes.Structure):
+    _fields_ = [("algorithm", ctypes.c_char_p), ("data_layout", ctypes.c_char_p), ("debug_mode", ctypes.c_int),
+                ("work_group_size", ctypes.c_uint), ("time_steps", ctypes.c_uint),
+                ("frame_update_interval", ctypes.c_uint), ("scenario", ctypes.c_char_p),
+                ("vertical_nodes", ctypes.c_uint), ("horizontal_nodes", ctypes.c_uint),
+                ("inlet_velocity_x", ctypes.c_double), ("inlet_velocity_y", ctypes.c_double),
+                ("inlet_density", ctypes.c_double), ("outlet_velocity_x", ctypes.c_double),
+                ("outlet_velocity_y", ctypes.c_double), ("outlet_density", ctypes.c_double),
+                ("relaxation_time", ctypes.c_double)]
+
+
+class _COpts(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("nan_protection", ctypes.c_int), ("use_graph", ctypes.c_int),
+                ("device", ctypes.c_int), ("mask", ctypes.c_void_p)]
+
+
+def library_path() -> str:
+    return os.path.join(_HERE, "libplbm.so")
+
+
+_LIB = None
+
+# Exported symbols of include/plbm_c.h with their argument types.
+_SIGS = {
+    "plbm_default_options": (None, [ctypes.POINTER(_COpts)]),
+    "plbm_validate": (ctypes.c_int, [ctypes.POINTER(_CProps)]),
+    "plbm_create": (ctypes.c_int, [ctypes.POINTER(_CProps), ctypes.POINTER(_COpts), ctypes.POINTER(ctypes.c_void_p)]),
+    "plbm_create_from_json": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_COpts), ctypes.POINTER(ctypes.c_void_p)]),
+    "plbm_destroy": (None, [ctypes.c_void_p]),
+    "plbm_initialize": (ctypes.c_int, [ctypes.c_void_p]),
+    "plbm_start": (ctypes.c_int, [ctypes.c_void_p]),
+    "plbm_pause": (ctypes.c_int, [ctypes.c_void_p]),
+    "plbm_block_until_finished": (ctypes.c_int, [ctypes.c_void_p]),
+    "plbm_is_finished": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "plbm_get_results": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)),
+                                        ctypes.POINTER(ctypes.c_size_t)]),
+    "plbm_get_extents": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_uint)]),
+    "plbm_get_domain": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]),
+    "plbm_get_progress": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "plbm_get_last_frametime": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "plbm_get_current_iteration": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]),
+    "plbm_get_properties": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(_CProps)]),
+    "plbm_properties_to_json": (ctypes.c_int, [ctypes.POINTER(_CProps), ctypes.c_char_p]),
+    "plbm_json_to_properties": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_CProps)]),
+    "plbm_run_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint, ctypes.POINTER(ctypes.c_double)]),
+    "plbm_sync_results": (ctypes.c_int, [ctypes.c_void_p]),
+    "plbm_launches_per_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]),
+    "plbm_bytes_per_node": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "plbm_mass_momentum": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "plbm_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "plbm_version": (ctypes.c_char_p, []),
+}
+
+
+def load_library() -> ctypes.CDLL:
+    """Loads the in-tree libplbm.so; raises if it has not been built (no fallback path)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -m portlbm_gb300.build`")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _check(rc: int, handle=None) -> None:
+    if rc == 0:
+        return
+    lib = load_library()
+    msg = lib.plbm_last_error(handle).decode(errors="replace")
+    raise _CODES.get(rc, Exception)(msg)
+
+
+class Properties:
+    """core::Properties; ``vertical_nodes``/``horizontal_nodes`` are passed as inner extents and
+    stored with the two ghost layers added (src/lbm/core/simulation.cpp:45-48)."""
+
+    def __init__(self, algorithm: str, data_layout: str, debug_mode: bool, work_group_size: int,
+                 time_steps: int, frame_update_interval: int, scenario: str, vertical_nodes: int,
+                 horizontal_nodes: int, inlet_velocity_x: float, inlet_velocity_y: float,
+                 inlet_density: float, outlet_velocity_x: float, outlet_velocity_y: float,
+                 outlet_density: float, relaxation_time: float):
+        self.algorithm = algorithm
+        self.data_layout = data_layout
+        self.debug_mode = bool(debug_mode)
+        self.work_group_size = int(work_group_size)
+        self.time_steps = int(time_steps)
+        self.frame_update_interval = int(frame_update_interval)
+        self.scenario = scenario
+        self.vertical_nodes = int(vertical_nodes) + 2
+        self.horizontal_nodes = int(horizontal_nodes) + 2
+        self.total_unexpanded_node_count = self.vertical_nodes * self.horizontal_nodes
+        self.domain_node_count = int(vertical_nodes) * int(horizontal_nodes)
+        self.inlet_velocity_x = float(inlet_velocity_x)
+        self.inlet_velocity_y = float(inlet_velocity_y)
+        self.inlet_density = float(inlet_density)
+        self.outlet_velocity_x = float(outlet_velocity_x)
+        self.outlet_velocity_y = float(outlet_velocity_y)
+        self.outlet_density = float(outlet_density)
+        self.relaxation_time = float(relaxation_time)
+        self.settings_path = ""
+
+    def _c(self) -> _CProps:
+        self._keep = [s.encode() for s in (self.algorithm, self.data_layout, self.scenario)]
+        return _CProps(self._keep[0], self._keep[1], int(self.debug_mode), self.work_group_size, self.time_steps,
+                       self.frame_update_interval, self._keep[2], self.vertical_nodes - 2,
+                       self.horizontal_nodes - 2, self.inlet_velocity_x, self.inlet_velocity_y,
+                       self.inlet_density, self.outlet_velocity_x, self.outlet_velocity_y, self.outlet_density,
+                       self.relaxation_time)
+
+    @classmethod
+    def _from_c(cls, c: _CProps, path: str = "") -> "Properties":
+        p = cls(c.algorithm.decode(), c.data_layout.decode(), bool(c.debug_mode), c.work_group_size, c.time_steps,
+                c.frame_update_interval, c.scenario.decode(), c.vertical_nodes, c.horizontal_nodes,
+                c.inlet_velocity_x, c.inlet_velocity_y, c.inlet_density, c.outlet_velocity_x, c.outlet_velocity_y,
+                c.outlet_density, c.relaxation_time)
+        p.settings_path = path
+        return p
+
+    def validate(self) -> None:
+        """Properties::validate (src/lbm/core/simulation.cpp:60-125)."""
+        c = self._c()
+        _check(load_library().plbm_validate(ctypes.byref(c)))
+
+    def to_string(self) -> str:
+        """Properties::to_string (src/lbm/core/simulation.cpp:137-175)."""
+        return ("Algorithmic properties: \n"
+                f"\tAlgorithm: {self.algorithm} \n\tData layout: {self.data_layout} \n"
+                f"\tWork group size: {self.work_group_size} \n\tDebug mode: {str(self.debug_mode).lower()} \n"
+                f"\tTime steps: {self.time_steps} \n\tFrame update interval: {self.frame_update_interval} \n"
+                "Domain properties: \n"
+                f"\tScenario: {self.scenario}\n\tVertical nodes: {self.vertical_nodes} \n"
+                f"\tHorizontal nodes: {self.horizontal_nodes} \n\tNode count: {self.total_unexpanded_node_count} \n"
+                "Physical: \n"
+                f"\tInlet velocity: ({self.inlet_velocity_x:.6f}, {self.inlet_velocity_y:.6f})\n"
+                f"\tInlet density: {self.inlet_density:.6f}\n"
+                f"\tOutlet velocity: ({self.outlet_velocity_x:.6f}, {self.outlet_velocity_y:.6f})\n"
+                f"\tOutlet density: {self.outlet_density:.6f}\n"
+                f"\tRelaxation time: {self.relaxation_time:.6f}\n\n")
+
+
+def properties_to_json(props: Properties, path: str) -> None:
+    """file_interaction::properties_to_json (src/lbm/file_interaction/file_interaction.cpp:11-37),
+    writing the inner node counts."""
+    c = props._c()
+    _check(load_library().plbm_properties_to_json(ctypes.byref(c), path.encode()))
+
+
+def json_to_properties(path: str, offset: int = 0) -> Properties:
+    """file_interaction::json_to_properties (file_interaction.cpp:39-69)."""
+    c = _CProps()
+    _check(load_library().plbm_json_to_properties(path.encode(), int(offset), ctypes.byref(c)))
+    return Properties._from_c(c, path)
+
+
+class AlgorithmHandler:
+    """execution::AlgorithmHandler backed by a libplbm handle."""
+
+    def __init__(self, handle: int):
+        self._lib = load_library()
+        self._h = ctypes.c_void_p(handle)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.plbm_destroy(h)
+            self._h = None
+
+    def close(self) -> None:
+        self.__del__()
+
+    def _call(self, name: str, *args):
+        _check(getattr(self._lib, name)(self._h, *args), self._h)
+
+    # -- life cycle (algorithm_handler.hpp:55-88) --
+    def initialize(self) -> None:
+        self._call("plbm_initialize")
+
+    def start(self) -> None:
+        self._call("plbm_start")
+
+    def pause(self) -> None:
+        self._call("plbm_pause")
+
+    def block_until_finished(self) -> None:
+        self._call("plbm_block_until_finished")
+
+    def is_finished(self) -> bool:
+        v = ctypes.c_int()
+        self._call("plbm_is_finished", ctypes.byref(v))
+        return bool(v.value)
+
+    # -- results (algorithm_handler.hpp:90-121) --
+    def _result(self, which: int, copy: bool = True) -> np.ndarray:
+        ptr = ctypes.POINTER(ctypes.c_double)()
+        n = ctypes.c_size_t()
+        self._call("plbm_get_results", which, ctypes.byref(ptr), ctypes.byref(n))
+        arr = np.ctypeslib.as_array(ptr, shape=(n.value,))
+        return arr.copy() if copy else arr
+
+    def get_densities(self, copy: bool = True) -> np.ndarray:
+        return self._result(0, copy)
+
+    def get_x_velocities(self, copy: bool = True) -> np.ndarray:
+        return self._result(1, copy)
+
+    def get_y_velocities(self, copy: bool = True) -> np.ndarray:
+        return self._result(2, copy)
+
+    def get_absolute_velocities(self, copy: bool = True) -> np.ndarray:
+        return self._result(3, copy)
+
+    # -- extents and status (algorithm_handler.hpp:123-151) --
+    def get_horizontal_nodes(self) -> int:
+        h, v = ctypes.c_uint(), ctypes.c_uint()
+        self._call("plbm_get_extents", ctypes.byref(h), ctypes.byref(v))
+        return h.value
+
+    def get_vertical_nodes(self) -> int:
+        h, v = ctypes.c_uint(), ctypes.c_uint()
+        self._call("plbm_get_extents", ctypes.byref(h), ctypes.byref(v))
+        return v.value
+
+    def get_properties(self) -> Properties:
+        c = _CProps()
+        self._call("plbm_get_properties", ctypes.byref(c))
+        return Properties._from_c(c)
+
+    def get_inlet_density(self) -> float:
+        return self.get_properties().inlet_density
+
+    def get_outlet_density(self) -> float:
+        return self.get_properties().outlet_density
+
+    def get_domain(self) -> dict:
+        arr = (ctypes.c_uint * 7)()
+        self._call("plbm_get_domain", arr)
+        keys = ("total_node_count", "horizontal_nodes", "vertical_nodes", "subdomain_vertical_nodes",
+                "subdomain_horizontal_nodes", "subdomain_count_vertical", "subdomain_count_horizontal")
+        return dict(zip(keys, list(arr)))
+
+    def get_progress(self) -> float:
+        v = ctypes.c_double()
+        self._call("plbm_get_progress", ctypes.byref(v))
+        return v.value
+
+    def get_last_frametime(self) -> float:
+        v = ctypes.c_double()
+        self._call("plbm_get_last_frametime", ctypes.byref(v))
+        return v.value
+
+    def get_current_iteration(self) -> int:
+        v = ctypes.c_uint()
+        self._call("plbm_get_current_iteration", ctypes.byref(v))
+        return v.value
+
+    # -- measurement hooks (no counterpart in the reference) --
+    def run_steps(self, n: int) -> float:
+        """Runs n steps synchronously with device-resident data; returns device ms per step."""
+        ms = ctypes.c_double()
+        self._call("plbm_run_steps", int(n), ctypes.byref(ms))
+        return ms.value
+
+    def sync_results(self) -> None:
+        self._call("plbm_sync_results")
+
+    def mass_momentum(self) -> tuple:
+        out = (ctypes.c_double * 3)()
+        self._call("plbm_mass_momentum", out)
+        return tuple(out)
+
+    def bytes_per_node(self) -> float:
+        v = ctypes.c_double()
+        self._call("plbm_bytes_per_node", ctypes.byref(v))
+        return v.value
+
+    def launches_per_step(self) -> int:
+        v = ctypes.c_uint()
+        self._call("plbm_launches_per_step", ctypes.byref(v))
+        return v.value
+
+
+def create_handler(source, precision: str = "f64_strict", mask=None, nan_protection: bool = True,
+                   use_graph: bool = True, device: int = 0) -> AlgorithmHandler:
+    """lbm::create_handler from a ``Properties`` or a settings.json path.
+
+    ``precision`` picks the arithmetic form ("f64_strict" is the drop-in); ``mask`` is an optional
+    (H, W) array of 0 (fluid) / 1 (solid) replacing walls and scenario geometry.
+    """
+    lib = load_library()
+    opts = _COpts()
+    lib.plbm_default_options(ctypes.byref(opts))
+    opts.precision = PRECISIONS[precision]
+    opts.nan_protection = int(bool(nan_protection))
+    opts.use_graph = int(bool(use_graph))
+    opts.device = int(device)
+    keep = None
+    if mask is not None:
+        keep = np.ascontiguousarray(mask, dtype=np.int8)
+        opts.mask = keep.ctypes.data
+    out = ctypes.c_void_p()
+    if isinstance(source, Properties):
+        c = source._c()
+        rc = lib.plbm_create(ctypes.byref(c), ctypes.byref(opts), ctypes.byref(out))
+    else:
+        if precision == "f64_strict":
+            opts.precision = 0
+        rc = lib.plbm_create_from_json(str(source).encode(), ctypes.byref(opts), ctypes.byref(out))
+    _check(rc)
+    del keep
+    return AlgorithmHandler(out.value)

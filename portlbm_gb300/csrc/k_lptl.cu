@@ -1,0 +1,14 @@
+// k_lptl.cu — instantiations of the lptl step kernel (two lattices, 1-D launch).
+#include "plbm_dispatch.cuh"
+#include "plbm_launch.h"
+
+namespace plbm {
+cudaError_t launch_lptl(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s)
+{
+    switch (prec * 3 + lay) {
+        PLBM_ALL_CASES(k_lptl)
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+}  // namespace plbm

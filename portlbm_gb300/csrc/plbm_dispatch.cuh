@@ -1,0 +1,12 @@
+// plbm_dispatch.cuh — maps runtime (precision, layout) to a template instantiation.
+#pragma once
+#include "plbm_kernels.cuh"
+
+#define PLBM_CASE(KER, PR, LA) case (PR) * 3 + (LA): KER<PR, LA><<<grid, block, 0, s>>>(p); break;
+#define PLBM_ALL_CASES(KER)                                                                   \
+    PLBM_CASE(KER, 0, 0) PLBM_CASE(KER, 0, 1) PLBM_CASE(KER, 0, 2)                             \
+    PLBM_CASE(KER, 1, 0) PLBM_CASE(KER, 1, 1) PLBM_CASE(KER, 1, 2)                             \
+    PLBM_CASE(KER, 2, 0) PLBM_CASE(KER, 2, 1) PLBM_CASE(KER, 2, 2)                             \
+    PLBM_CASE(KER, 3, 0) PLBM_CASE(KER, 3, 1) PLBM_CASE(KER, 3, 2)                             \
+    PLBM_CASE(KER, 4, 0) PLBM_CASE(KER, 4, 1) PLBM_CASE(KER, 4, 2)                             \
+    PLBM_CASE(KER, 5, 0) PLBM_CASE(KER, 5, 1) PLBM_CASE(KER, 5, 2)

@@ -1,0 +1,965 @@
+// plbm_host.cpp — host side of libplbm: the C ABI declared in include/plbm_c.h.
+//
+// Mirrors, in C++ on top of hand-written sm_103a kernels, the reference's host path
+// (SC-SGS/PortLBM): Properties and its validation (src/lbm/core/simulation.cpp:21-125),
+// Domain arithmetic (:194-382), settings.json I/O (src/lbm/file_interaction/
+// file_interaction.cpp:11-69), geometry set-up (include/lbm/core/domain_initialization.hpp),
+// and the SYCLAlgorithmHandler life cycle (include/lbm/execution/sycl_algorithm_handler.hpp:
+// 252-455) with its per-step loop (include/lbm/gpu/nptl/nptl.hpp:116-141 and twins).
+//
+// Differences by design: one fused kernel launch per timestep instead of 3-7 launches each
+// followed by a host wait; observables are written on the steps that are copied to the host
+// (every other step's values are overwritten before any copy in the reference); runs of steps
+// between copies are replayed from a captured CUDA graph.
+#include "../../include/plbm_c.h"
+#include "plbm_json.hpp"
+#include "plbm_launch.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+using plbm::Json;
+using plbm::JsonError;
+
+struct Status {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string &msg) { throw Status{ code, msg }; }
+
+void cuda_check(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) fail(PLBM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// ---- core::Properties (include/lbm/core/properties.hpp:30-166) ---------------------------
+
+struct Props {
+    std::string algorithm, data_layout, scenario, settings_path;
+    bool debug_mode = false;
+    unsigned work_group_size = 0, time_steps = 0, frame_update_interval = 0;
+    unsigned vertical_nodes = 0, horizontal_nodes = 0;   // stored extents: inner + 2
+    unsigned total_unexpanded_node_count = 0, domain_node_count = 0;
+    double ivx = 0, ivy = 0, irho = 0, ovx = 0, ovy = 0, orho = 0, tau = 0;
+
+    // Properties::Properties (simulation.cpp:21-58): inner extents in, ghost layers added.
+    static Props make(const plbm_properties &c)
+    {
+        Props p;
+        p.algorithm = c.algorithm ? c.algorithm : "";
+        p.data_layout = c.data_layout ? c.data_layout : "";
+        p.scenario = c.scenario ? c.scenario : "";
+        p.debug_mode = c.debug_mode != 0;
+        p.work_group_size = c.work_group_size;
+        p.time_steps = c.time_steps;
+        p.frame_update_interval = c.frame_update_interval;
+        p.vertical_nodes = c.vertical_nodes + 2;
+        p.horizontal_nodes = c.horizontal_nodes + 2;
+        p.total_unexpanded_node_count = (c.vertical_nodes + 2) * (c.horizontal_nodes + 2);
+        p.domain_node_count = c.vertical_nodes * c.horizontal_nodes;
+        p.ivx = c.inlet_velocity_x; p.ivy = c.inlet_velocity_y; p.irho = c.inlet_density;
+        p.ovx = c.outlet_velocity_x; p.ovy = c.outlet_velocity_y; p.orho = c.outlet_density;
+        p.tau = c.relaxation_time;
+        return p;
+    }
+
+    // Properties::validate (simulation.cpp:60-125), same checks, order and messages.
+    void validate() const
+    {
+        static const char *algs[] = { "nptl", "lptl", "npol", "nsol" };
+        static const char *lays[] = { "stream", "collision", "bundle" };
+        static const char *scns[] = { "Hagen-Poiseuille", "walls", "circle", "square", "plate", "skyscraper", "wing", "porous" };
+        if (vertical_nodes < 4) fail(PLBM_ERR_PROPERTY, "vertical_nodes must be >= 4 (inner domain >= 2 rows)");
+        if (horizontal_nodes < 4) fail(PLBM_ERR_PROPERTY, "horizontal_nodes must be >= 4 (inner domain >= 2 cols)");
+        if (time_steps < 1) fail(PLBM_ERR_PROPERTY, "time_steps must be >= 1");
+        if (frame_update_interval < 1) fail(PLBM_ERR_PROPERTY, "frame_update_interval must be >= 1");
+        if (work_group_size < 1) fail(PLBM_ERR_PROPERTY, "work_group_size must be >= 1");
+        if (irho <= 0) fail(PLBM_ERR_PROPERTY, "inlet_density must be > 0");
+        if (orho <= 0) fail(PLBM_ERR_PROPERTY, "outlet_density must be > 0");
+        if (tau <= 0) fail(PLBM_ERR_PROPERTY, "relaxation_time must be > 0");
+        auto in = [](const std::string &v, const char *const *l, int n) {
+            for (int i = 0; i < n; ++i)
+                if (v == l[i]) return true;
+            return false;
+        };
+        if (!in(algorithm, algs, 4))
+            fail(PLBM_ERR_PROPERTY, "Unknown algorithm: \"" + algorithm + "\". Valid values: lptl, nptl, npol, nsol");
+        if (!in(data_layout, lays, 3))
+            fail(PLBM_ERR_PROPERTY,
+                 "Unknown data_layout: \"" + data_layout + "\". Valid values: stream, collision, bundle");
+        if (!in(scenario, scns, 8))
+            fail(PLBM_ERR_PROPERTY, "Unknown scenario: \"" + scenario +
+                                        "\". Valid values: Hagen-Poiseuille, walls, circle, square, plate, skyscraper, wing, porous");
+    }
+
+    plbm_properties to_c() const
+    {
+        plbm_properties c{};
+        c.algorithm = algorithm.c_str(); c.data_layout = data_layout.c_str(); c.scenario = scenario.c_str();
+        c.debug_mode = debug_mode; c.work_group_size = work_group_size; c.time_steps = time_steps;
+        c.frame_update_interval = frame_update_interval;
+        c.vertical_nodes = vertical_nodes - 2; c.horizontal_nodes = horizontal_nodes - 2;
+        c.inlet_velocity_x = ivx; c.inlet_velocity_y = ivy; c.inlet_density = irho;
+        c.outlet_velocity_x = ovx; c.outlet_velocity_y = ovy; c.outlet_density = orho;
+        c.relaxation_time = tau;
+        return c;
+    }
+};
+
+// ---- settings.json (file_interaction.cpp:11-69) -----------------------------------------
+
+std::string read_file(const std::string &path)
+{
+    std::ifstream f(path, std::ios::binary);
+    if (!f) fail(PLBM_ERR_PARSE, "parse_error: cannot open settings file '" + path + "'");
+    std::stringstream ss;
+    ss << f.rdbuf();
+    return ss.str();
+}
+
+struct JsonExtras {
+    int precision = -1;
+    int nan_protection = -1;
+};
+
+int precision_from_name(const std::string &s)
+{
+    static const char *names[] = { "f64_strict", "f64_fast", "f32_ref", "f32", "f16s", "bf16s" };
+    for (int i = 0; i < 6; ++i)
+        if (s == names[i]) return i;
+    fail(PLBM_ERR_PROPERTY, "Unknown gb300.precision: \"" + s + "\". Valid values: f64_strict, f64_fast, f32_ref, f32, f16s, bf16s");
+}
+
+// json_to_properties(path, offset): the node counts read are inner extents plus `offset`, and the
+// Properties constructor adds the two ghost layers.
+Props json_to_props(const std::string &path, int offset, JsonExtras *extras)
+{
+    const std::string text = read_file(path);
+    try {
+        const Json root = plbm::JsonParser(text).parse();
+        const Json &a = root.at("algorithmic"), &d = root.at("domain"), &ph = root.at("physical");
+        plbm_properties c{};
+        std::string alg = a.at("algorithm").as_string(), lay = a.at("dataLayout").as_string();
+        c.debug_mode = a.at("debugMode").as_bool();
+        c.work_group_size = a.at("workGroupSize").as_unsigned();
+        c.time_steps = a.at("timeSteps").as_unsigned();
+        c.frame_update_interval = a.at("frameUpdateInterval").as_unsigned();
+        std::string scn = d.at("scenario").as_string();
+        c.vertical_nodes = d.at("verticalNodes").as_unsigned() + (unsigned)offset;
+        c.horizontal_nodes = d.at("horizontalNodes").as_unsigned() + (unsigned)offset;
+        c.inlet_velocity_x = ph.at("inletVelocity").at("x").as_double();
+        c.inlet_velocity_y = ph.at("inletVelocity").at("y").as_double();
+        c.inlet_density = ph.at("inletDensity").as_double();
+        c.outlet_velocity_x = ph.at("outletVelocity").at("x").as_double();
+        c.outlet_velocity_y = ph.at("outletVelocity").at("y").as_double();
+        c.outlet_density = ph.at("outletDensity").as_double();
+        c.relaxation_time = ph.at("relaxationTime").as_double();
+        c.algorithm = alg.c_str(); c.data_layout = lay.c_str(); c.scenario = scn.c_str();
+        Props p = Props::make(c);
+        p.settings_path = path;
+        if (extras) {
+            if (const Json *g = root.find("gb300")) {
+                if (const Json *pr = g->find("precision")) extras->precision = precision_from_name(pr->as_string());
+                if (const Json *np = g->find("nanProtection")) extras->nan_protection = np->as_bool() ? 1 : 0;
+            }
+        }
+        return p;
+    } catch (const JsonError &e) {
+        fail(PLBM_ERR_PARSE, e.what());
+    }
+}
+
+// properties_to_json (file_interaction.cpp:11-37): writes the given node counts as they are.
+void props_to_json(const Props &p, unsigned vnodes, unsigned hnodes, const std::string &path)
+{
+    Json root;
+    Json &a = root.set("algorithmic");
+    a.set("workGroupSize") = plbm::jnum(p.work_group_size, true);
+    a.set("debugMode") = plbm::jbool(p.debug_mode);
+    a.set("timeSteps") = plbm::jnum(p.time_steps, true);
+    a.set("dataLayout") = plbm::jstr(p.data_layout);
+    a.set("algorithm") = plbm::jstr(p.algorithm);
+    a.set("frameUpdateInterval") = plbm::jnum(p.frame_update_interval, true);
+    Json &d = root.set("domain");
+    d.set("scenario") = plbm::jstr(p.scenario);
+    d.set("verticalNodes") = plbm::jnum(vnodes, true);
+    d.set("horizontalNodes") = plbm::jnum(hnodes, true);
+    Json &ph = root.set("physical");
+    Json &iv = ph.set("inletVelocity");
+    iv.set("x") = plbm::jnum(p.ivx, false);
+    iv.set("y") = plbm::jnum(p.ivy, false);
+    ph.set("inletDensity") = plbm::jnum(p.irho, false);
+    Json &ov = ph.set("outletVelocity");
+    ov.set("x") = plbm::jnum(p.ovx, false);
+    ov.set("y") = plbm::jnum(p.ovy, false);
+    ph.set("outletDensity") = plbm::jnum(p.orho, false);
+    ph.set("relaxationTime") = plbm::jnum(p.tau, false);
+    std::string out;
+    plbm::json_dump(out, root);
+    std::ofstream f(path);
+    f << out;
+}
+
+// ---- core::Domain (simulation.cpp:194-382; power functions simulation.hpp:373-446) -----------
+
+struct Domain {
+    unsigned total_node_count, horizontal_nodes, vertical_nodes, subdomain_vertical_nodes,
+        subdomain_horizontal_nodes, subdomain_count_vertical, subdomain_count_horizontal;
+};
+
+size_t which_power_of_4(size_t x)
+{
+    size_t checkbit = 3, pow = 0;
+    if ((x & 0x1) || x == 0) return 0;
+    while (!(checkbit & x)) { x >>= 2; pow++; }
+    return !(x & 2) ? pow : 0;
+}
+
+size_t which_power_of_2(size_t x)
+{
+    size_t checkbit = 1, pow = 0;
+    if ((x & 0x1) || x == 0) return 0;
+    while (!(checkbit & x)) { x >>= 1; pow++; }
+    return !(x >> 1 | 0) ? pow : 0;
+}
+
+void power_of_two_handling(size_t wg, unsigned &sv, unsigned &sh)
+{
+    const size_t p4 = which_power_of_4(wg), p2 = which_power_of_2(wg);
+    if (p4) {
+        size_t size = 1;
+        for (size_t i = 0; i < p4; ++i) size *= 2;
+        sh = sv = (unsigned)size;
+    } else if (p2) {
+        size_t height = 1;
+        for (size_t i = 0; i < p2 / 2; ++i) height *= 2;
+        sv = (unsigned)height;
+        sh = (unsigned)(2 * height);
+    } else {
+        sv = 2;
+        sh = (unsigned)(wg / 2);
+    }
+}
+
+void subdomain_count(unsigned ext, unsigned sub, unsigned &c)
+{
+    c = ((ext - 2) / sub) + 1;
+    if (!((ext - 2) % sub)) c--;
+}
+
+// Returns false when nsol's work-group size is below its minimum of 6.
+bool make_domain(const Props &p, Domain &d)
+{
+    const unsigned X = p.horizontal_nodes, V = p.vertical_nodes;
+    d = Domain{ X * V, X, V, V, X, 1, 1 };
+    if (p.algorithm == "lptl") return true;
+    unsigned sv, sh;
+    size_t w = p.work_group_size;
+    if (p.algorithm == "nsol") {
+        if (w < 6) return false;
+        if (w & 0x1) w--;
+        power_of_two_handling(w, sv, sh);
+        sv -= 1;
+        sh -= 2;
+    } else if (w & 0x1) {
+        sh = (unsigned)w;
+        sv = 1;
+    } else {
+        power_of_two_handling(w, sv, sh);
+    }
+    d.subdomain_vertical_nodes = sv;
+    d.subdomain_horizontal_nodes = sh;
+    subdomain_count(V, sv, d.subdomain_count_vertical);
+    subdomain_count(X, sh, d.subdomain_count_horizontal);
+    if (p.algorithm == "nptl") {
+        d.vertical_nodes = sv * d.subdomain_count_vertical + 2;
+        d.horizontal_nodes = sh * d.subdomain_count_horizontal + 2;
+    } else {
+        d.vertical_nodes = (sv + 1) * d.subdomain_count_vertical + 1;
+        d.horizontal_nodes = (sh + 1) * d.subdomain_count_horizontal + 1;
+    }
+    d.total_node_count = d.vertical_nodes * d.horizontal_nodes;
+    return true;
+}
+
+// ---- geometry (domain_initialization.hpp:41-297, :453-518) -------------------------------
+
+unsigned stencil(const std::string &sc, unsigned x, unsigned y, unsigned V, unsigned X)
+{
+    if (sc == "walls") {
+        unsigned cond = (x == (1 * X) / 6 || x == (3 * X) / 6 || x == (5 * X) / 6) && (y > 1) && (y < V / 2);
+        cond += (x == (2 * X) / 6 || x == (4 * X) / 6) && (y < V - 2) && (y > ((V - 1) / 2));
+        return cond;
+    }
+    if (sc == "circle") {
+        const unsigned mx = 2 * X / 10, my = V / 2, r = V / 5, dx = mx - x, dy = my - y;
+        return (y >= my - r) && (y <= my + r) && (x >= mx - r) && (x <= mx + r) && (dx * dx + dy * dy <= r * r);
+    }
+    if (sc == "square") {
+        const unsigned mx = 2 * X / 10, my = V / 2, hl = V / 10;
+        return (y >= my - hl) && (y <= my + hl) && (x >= mx - hl) && (x <= mx + hl);
+    }
+    if (sc == "plate") {
+        const unsigned mx = X / 10, my = V / 2, hh = 7 * V / 40, hw = hh / 60;
+        return (y >= my - hh) && (y <= my + hh) && (x >= mx - hw) && (x <= mx + hw);
+    }
+    if (sc == "skyscraper") {
+        const unsigned ha = V / 2, hwa = 1, hs = 2 * V / 5, hws = V / 24, hf = V / 4, hwf = V / 16, mx = 3 * X / 10;
+        return ((y >= 1) && (y <= hf && x >= mx - hwf && x <= mx + hwf)) ||
+               (y <= hs && x >= mx - hws && x <= mx + hws) || (y <= ha && x >= mx - hwa && x <= mx + hwa);
+    }
+    if (sc == "wing") {
+        const int mx = (int)(X / 5), my = (int)(V / 2), rmax = (int)(V / 5), sy = 5;
+        const unsigned ddx = x - (unsigned)mx, ddy = y - (unsigned)my;
+        return ((0.2 * (double)(ddx * ddx) + (double)(ddy * ddy)) <= rmax) ||
+               ((std::pow((double)ddx, 1.4) + (double)((unsigned)(sy * sy) * (ddy * ddy))) <= sy * sy * rmax);
+    }
+    return 0;  // Hagen-Poiseuille
+}
+
+// Inner W*H flag grid (0 fluid, 1 solid) in reference coordinates (x, y) -> (x-1, y-1).
+std::vector<int8_t> make_flags(const Props &p, const std::vector<int8_t> *mask)
+{
+    const unsigned X = p.horizontal_nodes, V = p.vertical_nodes, W = X - 2, H = V - 2;
+    std::vector<int8_t> f((size_t)W * H, -1);
+    auto at = [&](unsigned x, unsigned y) -> int8_t & { return f[(size_t)(x - 1) + (size_t)(y - 1) * W]; };
+    if (mask) {
+        for (size_t i = 0; i < f.size(); ++i) f[i] = (*mask)[i];
+        return f;
+    }
+    if (p.scenario == "porous") {
+        // porous_medium_mask :265-297 draws from the process-wide std::rand() sequence.
+        for (int y = 2; (unsigned)y < V - 2; ++y)
+            for (int x = 1; (unsigned)x <= X - 2; ++x) {
+                const int one = 1 + (std::rand() % 10), two = 1 + (std::rand() % 10);
+                at((unsigned)x, (unsigned)y) = (x % one == one - 1 && y % two == two - 1) ? 1 : 0;
+            }
+        for (int y = 1; (unsigned)y < V; y += (int)(V - 3))
+            for (int x = 1; (unsigned)x <= X - 2; ++x)
+                if ((unsigned)y <= V - 2) at((unsigned)x, (unsigned)y) = 1;
+        return f;
+    }
+    for (unsigned x = 1; x <= X - 2; ++x) { at(x, 1) = 1; at(x, V - 2) = 1; }   // set_pipe_boundaries :214-239
+    for (unsigned y = 2; y + 2 < V; ++y)                                         // add_stencil :414-440
+        for (unsigned x = 1; x + 1 < X; ++x) at(x, y) = (int8_t)stencil(p.scenario, x, y, V, X);
+    return f;
+}
+
+// maxwell_boltzmann_distribution (simulation.hpp:333-350), in real_type R.
+template <typename R>
+void maxwell_boltzmann(R ux, R uy, R rho, R *t)
+{
+    static const R W[9] = { (R)(1.0 / 36), (R)(1.0 / 9), (R)(1.0 / 36), (R)(1.0 / 9), (R)(4.0 / 9),
+                            (R)(1.0 / 9), (R)(1.0 / 36), (R)(1.0 / 9), (R)(1.0 / 36) };
+    for (int d = 0; d < 9; ++d) {
+        const int vx = (d % 3) - 1, vy = (d / 3) - 1;
+        t[d] = (R)(W[d] * (rho + 3 * (vx * ux + vy * uy) + 9.0 / 2 * std::pow((double)(vx * ux + vy * uy), 2) -
+                           3.0 / 2 * (ux * ux + uy * uy)));
+    }
+}
+
+int alg_index(const std::string &a) { return a == "nptl" ? 0 : a == "lptl" ? 1 : a == "npol" ? 2 : 3; }
+int layout_index(const std::string &l) { return l == "collision" ? 0 : l == "stream" ? 1 : 2; }
+size_t storage_bytes(int prec) { return prec <= 1 ? 8 : prec <= 3 ? 4 : 2; }
+
+thread_local std::string g_tls_error;
+std::mutex g_create_mu;
+std::string g_create_error;
+
+}  // namespace
+
+// ---- the handler --------------------------------------------------------------------------
+
+struct plbm_handler {
+    Props props;
+    std::string settings_path;
+    bool from_json = false;
+    plbm_options opt{};
+    bool opt_precision_set = false;
+    std::vector<int8_t> user_mask;
+    bool has_mask = false;
+    Domain dom{};
+    int alg = 0, lay = 0, prec = 0;
+    int W = 0, H = 0, P = 0;
+    unsigned long long N = 0;
+    int outlet_mode = 0;
+
+    cudaStream_t stream = nullptr;
+    void *lat[2] = { nullptr, nullptr };
+    uint16_t *links = nullptr;
+    int8_t *flags_d = nullptr;
+    double *res_d[4] = { nullptr, nullptr, nullptr, nullptr };
+    double *jy_d = nullptr;
+    void *halo[2] = { nullptr, nullptr };
+    double *red_d = nullptr;
+    double *res_h[4] = { nullptr, nullptr, nullptr, nullptr };
+    size_t nres = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    plbm::StepParams base{};
+    dim3 grid, block;
+    cudaGraphExec_t gexec = nullptr;
+    unsigned graph_steps = 0;
+
+    std::atomic<unsigned> iteration{ 0 };
+    std::atomic<bool> stop{ false };
+    std::atomic<double> progress{ 0.0 };
+    std::atomic<double> frametime{ 1.7976931348623157e308 };
+    std::thread worker;
+    bool active = false;
+    bool future_valid = true;
+    std::mutex mu;
+    int worker_status = PLBM_OK;
+    std::string worker_error;
+    std::string last_error;
+
+    ~plbm_handler() { release(); }
+
+    void release()
+    {
+        if (worker.joinable()) { stop = true; worker.join(); }
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+        for (auto &p : lat) { if (p) cudaFree(p); p = nullptr; }
+        for (auto &p : halo) { if (p) cudaFree(p); p = nullptr; }
+        for (auto &p : res_d) { if (p) cudaFree(p); p = nullptr; }
+        for (auto &p : res_h) { if (p) cudaFreeHost(p); p = nullptr; }
+        if (links) cudaFree(links);
+        if (flags_d) cudaFree(flags_d);
+        if (jy_d) cudaFree(jy_d);
+        if (red_d) cudaFree(red_d);
+        links = nullptr; flags_d = nullptr; jy_d = nullptr; red_d = nullptr;
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        ev0 = ev1 = nullptr;
+        if (stream) cudaStreamDestroy(stream);
+        stream = nullptr;
+    }
+
+    bool two_lattice() const { return alg == 0 || alg == 1; }
+
+    // SYCLAlgorithmHandler::initialize_algorithm (:252-272) + core::Simulation (simulation.cpp:
+    // 438-519) + setup_domain (domain_initialization.hpp:453-518).
+    void build()
+    {
+        release();
+        iteration = 0; progress = 0.0; frametime = 1.7976931348623157e308;
+        stop = false; active = false; future_valid = true; worker_status = PLBM_OK; worker_error.clear();
+        JsonExtras ex;
+        if (from_json) props = json_to_props(settings_path, 0, &ex);
+        // SYCLAlgorithmHandler::initialize_non_debug_algorithm (:75-157) rejects unknown names
+        // with exceptions::Exception; the remaining checks are Properties::validate()'s.
+        if (props.algorithm != "nptl" && props.algorithm != "lptl" && props.algorithm != "npol" && props.algorithm != "nsol")
+            fail(PLBM_ERR_UNKNOWN, "Unknown algorithm: " + props.algorithm);
+        if (props.data_layout != "stream" && props.data_layout != "collision" && props.data_layout != "bundle")
+            fail(PLBM_ERR_UNKNOWN, "Unknown data layout: " + props.data_layout);
+        props.validate();
+        prec = opt.precision;
+        if (ex.precision >= 0 && !opt_precision_set) prec = ex.precision;
+        if (ex.nan_protection >= 0) opt.nan_protection = ex.nan_protection;
+        if (prec < 0 || prec > 5) fail(PLBM_ERR_ARGUMENT, "precision must be one of PLBM_F64_STRICT..PLBM_BF16S");
+
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) fail(PLBM_ERR_NO_DEVICE, "no CUDA device available");
+        cuda_check(cudaSetDevice(opt.device), "cudaSetDevice");
+        int max_wg = 0;
+        cuda_check(cudaDeviceGetAttribute(&max_wg, cudaDevAttrMaxThreadsPerBlock, opt.device), "device attribute");
+        if (props.work_group_size > (unsigned)max_wg) {
+            const unsigned wrong = props.work_group_size;
+            if (from_json) {   // simulation.cpp:445-459: rewrite settings.json, then throw
+                Props q = props;
+                q.work_group_size = (unsigned)max_wg;
+                props_to_json(q, q.vertical_nodes - 2, q.horizontal_nodes - 2, settings_path);
+                fail(PLBM_ERR_PROPERTY, "Detected illegal work group size of " + std::to_string(wrong) +
+                                            " that exceeds the maximum work group size of " + std::to_string(max_wg) +
+                                            ". JSON property \"workGroupSize\" has been set to " + std::to_string(max_wg) +
+                                            " to enable graceful program restart. ");
+            }
+            fail(PLBM_ERR_PROPERTY, "work_group_size " + std::to_string(wrong) + " exceeds the device maximum of " +
+                                        std::to_string(max_wg) + "; reduce it to " + std::to_string(max_wg) +
+                                        " and reconstruct.");
+        }
+        if (!make_domain(props, dom)) {
+            // setup_for_swap simulation.cpp:336-353: re-read the settings, set 6, write back, throw.
+            if (props.settings_path.empty())
+                fail(PLBM_ERR_PARSE, "parse_error: settings file '' cannot be read to correct workGroupSize");
+            Props q = json_to_props(props.settings_path, -2, nullptr);
+            q.work_group_size = 6;
+            props_to_json(q, q.vertical_nodes, q.horizontal_nodes, props.settings_path);
+            fail(PLBM_ERR_PROPERTY, "Detected illegal work group size of " + std::to_string(props.work_group_size) +
+                                        " that is below the minimum work-group size of 6 of the swap algorithm. JSON "
+                                        "property \"workGroupSize\" has been set to 6 to enable graceful program restart. ");
+        }
+        alg = alg_index(props.algorithm);
+        lay = layout_index(props.data_layout);
+        W = (int)props.horizontal_nodes - 2;
+        H = (int)props.vertical_nodes - 2;
+        P = (W + 31) / 32 * 32;
+        N = (unsigned long long)P * H;
+        nres = (size_t)W * H;
+        // Buffered outlet border lookup (buffered.hpp:285-288) lands on a buffer column when the
+        // column X-3 closes a subdomain; the density outlet then never reaches the lattice and the
+        // outlet ghost keeps feq(outlet) (see the design doc for the derivation).
+        outlet_mode = 0;
+        if ((alg == 2 || alg == 3) && ((props.horizontal_nodes - 3) % dom.subdomain_horizontal_nodes) == 0) outlet_mode = 1;
+
+        if (has_mask) {
+            if (user_mask.size() != nres) fail(PLBM_ERR_ARGUMENT, "mask must hold inner W*H entries");
+            for (int8_t v : user_mask)
+                if (v != 0 && v != 1) fail(PLBM_ERR_ARGUMENT, "mask entries must be 0 (fluid) or 1 (solid)");
+        }
+        const std::vector<int8_t> flags = make_flags(props, has_mask ? &user_mask : nullptr);
+
+        cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
+        cuda_check(cudaEventCreate(&ev0), "event");
+        cuda_check(cudaEventCreate(&ev1), "event");
+        const size_t eb = storage_bytes(prec);
+        const size_t lat_bytes = 9ull * N * eb;
+        size_t free_b = 0, total_b = 0;
+        cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+        const size_t need = lat_bytes * (two_lattice() ? 2 : 1) + N * 2 + nres * (1 + 4 * 8);
+        if (need + (256ull << 20) > free_b)
+            fail(PLBM_ERR_CUDA, "out of device memory: need " + std::to_string(need >> 20) + " MiB, free " +
+                                    std::to_string(free_b >> 20) + " MiB");
+        for (int i = 0; i < (two_lattice() ? 2 : 1); ++i) cuda_check(cudaMalloc(&lat[i], lat_bytes), "cudaMalloc lattice");
+        cuda_check(cudaMalloc(&links, N * sizeof(uint16_t)), "cudaMalloc links");
+        cuda_check(cudaMalloc(&flags_d, nres), "cudaMalloc flags");
+        for (auto &r : res_d) cuda_check(cudaMalloc(&r, nres * sizeof(double)), "cudaMalloc results");
+        for (auto &r : res_h) cuda_check(cudaMallocHost(&r, nres * sizeof(double)), "cudaMallocHost results");
+        for (size_t i = 0; i < nres; ++i) { res_h[0][i] = -1.0; res_h[1][i] = 0; res_h[2][i] = 0; res_h[3][i] = 0; }
+        cuda_check(cudaMalloc(&jy_d, 2ull * H * sizeof(double)), "cudaMalloc jy");
+        cuda_check(cudaMemsetAsync(jy_d, 0, 2ull * H * sizeof(double), stream), "memset jy");
+        cuda_check(cudaMalloc(&red_d, 3 * sizeof(double)), "cudaMalloc reduce");
+        cuda_check(cudaMemcpyAsync(flags_d, flags.data(), nres, cudaMemcpyHostToDevice, stream), "H2D flags");
+        cuda_check(plbm::launch_links(flags_d, links, W, H, P, stream), "links kernel");
+        cuda_check(plbm::launch_fill_results(res_d[0], res_d[1], res_d[2], res_d[3], nres, stream), "results fill");
+
+        // Ghost constants and rest state in the arithmetic of the chosen form.
+        plbm::StepParams &b = base;
+        std::memset(&b, 0, sizeof b);
+        if (prec == PLBM_F64_STRICT || prec == PLBM_F64_FAST) {
+            maxwell_boltzmann<double>(0, 0, 1, b.weight);
+            maxwell_boltzmann<double>(props.ivx, props.ivy, props.irho, b.feq_in);
+            maxwell_boltzmann<double>(props.ovx, props.ovy, props.orho, b.feq_out);
+            b.omega = 1 / props.tau;
+            b.rho_out = props.orho;
+        } else {
+            float w[9], fi[9], fo[9];
+            maxwell_boltzmann<float>(0, 0, 1, w);
+            maxwell_boltzmann<float>((float)props.ivx, (float)props.ivy, (float)props.irho, fi);
+            maxwell_boltzmann<float>((float)props.ovx, (float)props.ovy, (float)props.orho, fo);
+            for (int d = 0; d < 9; ++d) { b.weight[d] = w[d]; b.feq_in[d] = fi[d]; b.feq_out[d] = fo[d]; }
+            b.omega = (double)(1 / (float)props.tau);
+            b.rho_out = (double)(float)props.orho;
+        }
+        for (int i = 0; i < (two_lattice() ? 2 : 1); ++i)
+            cuda_check(plbm::launch_fill_lattice(lat[i], prec, lay, N, b.weight, stream), "lattice fill");
+
+        b.links = links;
+        b.rho = res_d[0]; b.jx = res_d[1]; b.jy = res_d[2]; b.jabs = res_d[3];
+        b.W = W; b.H = H; b.P = P; b.N = N;
+        b.outlet_mode = outlet_mode;
+        b.nan_protection = opt.nan_protection;
+
+        // Launch shapes.  workGroupSize is honoured as a tile hint (core::Domain's subdomain shape),
+        // clamped to what the kernels can run; results do not depend on it.
+        const unsigned sh = dom.subdomain_horizontal_nodes, sv = dom.subdomain_vertical_nodes;
+        const int cap = plbm::max_threads_for(alg, prec, lay);
+        if (alg == 1) {
+            unsigned t = std::min<unsigned>(std::max<unsigned>(props.work_group_size, 32u), (unsigned)cap);
+            t = (t + 31) / 32 * 32;
+            block = dim3(t);
+            grid = dim3((unsigned)((N + t - 1) / t));
+        } else {
+            unsigned bx = alg == 0 || alg == 3 ? std::max(32u, std::min(sh, 128u)) : std::min(sh, 64u);
+            bx = std::max(1u, bx);
+            unsigned by = std::max(1u, std::min(sv, (unsigned)cap / bx));
+            if (alg == 2) {   // npol: one tile per block; tile edges carry the halo snapshots
+                bx = std::min(bx, (unsigned)W);
+                by = std::min(by, (unsigned)H);
+            }
+            block = dim3(bx, by);
+            grid = dim3((W + bx - 1) / bx, (H + by - 1) / by);
+        }
+        if (alg == 2) {
+            b.tile_w = (int)block.x;
+            b.tile_h = (int)block.y;
+            b.n_col_bounds = (int)grid.x - 1;
+            b.n_row_bounds = (int)grid.y - 1;
+            const size_t hn = (size_t)b.n_col_bounds * H * 6 + (size_t)b.n_row_bounds * W * 6;
+            for (auto &hp : halo) {
+                cuda_check(cudaMalloc(&hp, std::max<size_t>(hn, 1) * eb), "cudaMalloc halo");
+                cuda_check(plbm::launch_fill_halo(hp, prec, W, H, b.n_col_bounds, b.n_row_bounds, b.weight, stream),
+                           "halo fill");
+            }
+        }
+        cuda_check(cudaStreamSynchronize(stream), "initialisation");
+    }
+
+    cudaError_t launch_step(unsigned t, bool results)
+    {
+        plbm::StepParams p = base;
+        const unsigned par = t & 1u;
+        p.write_results = results ? 1 : 0;
+        p.lat0 = two_lattice() ? lat[par] : lat[0];
+        p.lat1 = two_lattice() ? lat[par ^ 1u] : nullptr;
+        p.jy_prev = jy_d + (size_t)par * H;
+        p.jy_next = jy_d + (size_t)(par ^ 1u) * H;
+        if (alg == 2) { p.halo_in = (double *)halo[par]; p.halo_out = (double *)halo[par ^ 1u]; }
+        switch (alg) {
+        case 0: return plbm::launch_nptl(prec, lay, p, grid, block, stream);
+        case 1: return plbm::launch_lptl(prec, lay, p, grid, block, stream);
+        case 2: return plbm::launch_npol(prec, lay, p, grid, block, stream);
+        default: return plbm::launch_nsol(prec, lay, p, t, grid, block, stream);
+        }
+    }
+
+    // Captures `pairs` (even, odd) step pairs without result writes into one executable graph.
+    void ensure_graph()
+    {
+        if (gexec || !opt.use_graph) return;
+        const unsigned pairs = N >= (1ull << 22) ? 4 : 32;
+        cudaGraph_t g = nullptr;
+        cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        cudaError_t e = cudaSuccess;
+        for (unsigned k = 0; k < 2 * pairs && e == cudaSuccess; ++k) e = launch_step(k, false);
+        cudaError_t e2 = cudaStreamEndCapture(stream, &g);
+        cuda_check(e, "capture launch");
+        cuda_check(e2, "end capture");
+        cuda_check(cudaGraphInstantiate(&gexec, g, 0), "graph instantiate");
+        cudaGraphDestroy(g);
+        graph_steps = 2 * pairs;
+    }
+
+    // Steps [t0, t1) with no result writes; graph replays where the parity allows.
+    void run_plain(unsigned t0, unsigned t1)
+    {
+        unsigned t = t0;
+        if (opt.use_graph && t1 - t0 >= 8) {
+            ensure_graph();
+            if (t & 1u) { cuda_check(launch_step(t, false), "step"); ++t; }
+            while (t + graph_steps <= t1) {
+                cuda_check(cudaGraphLaunch(gexec, stream), "graph launch");
+                t += graph_steps;
+            }
+        }
+        for (; t < t1; ++t) cuda_check(launch_step(t, false), "step");
+    }
+
+    void copy_results()
+    {
+        for (int i = 0; i < 4; ++i)
+            cuda_check(cudaMemcpyAsync(res_h[i], res_d[i], nres * sizeof(double), cudaMemcpyDeviceToHost, stream),
+                       "D2H results");
+        cuda_check(cudaStreamSynchronize(stream), "results copy");
+    }
+
+    // The per-step loop of the drivers (nptl.hpp:121-139): stop when paused or finished; results
+    // go to the host on frame steps and after the final step.
+    void loop()
+    {
+        try {
+            cuda_check(cudaSetDevice(opt.device), "cudaSetDevice");
+            const unsigned T = props.time_steps, F = props.frame_update_interval;
+            while (!stop.load() && iteration.load() < T) {
+                const unsigned t = iteration.load();
+                unsigned frame = t + (F - 1 - t % F);
+                if (frame > T - 1) frame = T - 1;
+                const auto c0 = std::chrono::steady_clock::now();
+                unsigned end;
+                if (t < frame) {
+                    const unsigned chunk = std::max<unsigned>(graph_steps ? graph_steps : 32, 32);
+                    end = std::min(frame, t + chunk);
+                    run_plain(t, end);
+                    cuda_check(cudaStreamSynchronize(stream), "step");
+                } else {
+                    cuda_check(launch_step(t, true), "step");
+                    copy_results();
+                    end = t + 1;
+                }
+                const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c0).count();
+                frametime = ms / (double)(end - t);
+                iteration = end;
+                progress = (double)end / (double)T;
+            }
+        } catch (const Status &s) {
+            std::lock_guard<std::mutex> g(mu);
+            worker_status = s.code;
+            worker_error = s.msg;
+        }
+    }
+};
+
+namespace {
+
+int set_err(plbm_handler *h, const Status &s)
+{
+    if (h) h->last_error = s.msg;
+    else {
+        std::lock_guard<std::mutex> g(g_create_mu);
+        g_create_error = s.msg;
+    }
+    return s.code;
+}
+
+template <typename F>
+int guarded(plbm_handler *h, F &&f)
+{
+    try {
+        f();
+        return PLBM_OK;
+    } catch (const Status &s) {
+        return set_err(h, s);
+    } catch (const std::exception &e) {
+        return set_err(h, Status{ PLBM_ERR_ARGUMENT, e.what() });
+    }
+}
+
+}  // namespace
+
+int plbm::max_threads_for(int alg, int prec, int lay)
+{
+    (void)alg; (void)lay;
+    return prec == PLBM_F64_STRICT || prec == PLBM_F32_REF ? 256 : 512;
+}
+
+extern "C" {
+
+void plbm_default_options(plbm_options *o)
+{
+    o->precision = PLBM_F64_STRICT;
+    o->nan_protection = 1;
+    o->use_graph = 1;
+    o->device = 0;
+    o->mask = nullptr;
+}
+
+int plbm_validate(const plbm_properties *props)
+{
+    return guarded(nullptr, [&] {
+        if (!props) fail(PLBM_ERR_ARGUMENT, "props is NULL");
+        Props::make(*props).validate();
+    });
+}
+
+static int create_common(plbm_handler *h, const plbm_options *opt, plbm_handler **out)
+{
+    if (opt) h->opt = *opt;
+    else plbm_default_options(&h->opt);
+    // A settings file's "gb300" object chooses the precision unless the caller's options name
+    // one other than the drop-in default.
+    h->opt_precision_set = opt && (!h->from_json || opt->precision != PLBM_F64_STRICT);
+    try {
+        if (h->opt.mask) {
+            Props p = h->from_json ? json_to_props(h->settings_path, 0, nullptr) : h->props;
+            const size_t n = (size_t)(p.horizontal_nodes - 2) * (p.vertical_nodes - 2);
+            h->user_mask.assign(h->opt.mask, h->opt.mask + n);
+            h->has_mask = true;
+            h->opt.mask = nullptr;
+        }
+        h->build();
+    } catch (const Status &s) {
+        set_err(nullptr, s);
+        delete h;
+        return s.code;
+    }
+    *out = h;
+    return PLBM_OK;
+}
+
+int plbm_create(const plbm_properties *props, const plbm_options *opt, plbm_handler **out)
+{
+    if (!props || !out) return set_err(nullptr, Status{ PLBM_ERR_ARGUMENT, "NULL argument" });
+    auto *h = new plbm_handler();
+    h->props = Props::make(*props);
+    return create_common(h, opt, out);
+}
+
+int plbm_create_from_json(const char *settings_path, const plbm_options *opt, plbm_handler **out)
+{
+    if (!settings_path || !out) return set_err(nullptr, Status{ PLBM_ERR_ARGUMENT, "NULL argument" });
+    auto *h = new plbm_handler();
+    h->from_json = true;
+    h->settings_path = settings_path;
+    return create_common(h, opt, out);
+}
+
+void plbm_destroy(plbm_handler *h) { delete h; }
+
+int plbm_initialize(plbm_handler *h)
+{
+    return guarded(h, [&] { h->build(); });
+}
+
+int plbm_start(plbm_handler *h)
+{
+    return guarded(h, [&] {
+        if (h->active) return;   // SYCLAlgorithmHandler::start :378-386
+        if (h->worker.joinable()) h->worker.join();
+        h->stop = false;
+        h->future_valid = true;
+        h->worker = std::thread([h] { h->loop(); });
+        h->active = true;
+    });
+}
+
+int plbm_pause(plbm_handler *h)
+{
+    return guarded(h, [&] {
+        h->stop = true;   // Control::forbid_execution; the step in flight completes
+        if (h->worker.joinable()) h->worker.join();
+        h->active = false;
+    });
+}
+
+int plbm_block_until_finished(plbm_handler *h)
+{
+    return guarded(h, [&] {
+        if (!h->future_valid)
+            fail(PLBM_ERR_WAIT, "A thread accessed a blocking statement causing it to wait for an algorithm that has "
+                                "not been launched.");
+        if (h->worker.joinable()) h->worker.join();
+        h->future_valid = false;
+        h->active = false;
+        std::lock_guard<std::mutex> g(h->mu);
+        if (h->worker_status != PLBM_OK) {
+            const Status s{ h->worker_status, h->worker_error };
+            h->worker_status = PLBM_OK;
+            throw s;
+        }
+    });
+}
+
+int plbm_is_finished(plbm_handler *h, int *finished)
+{
+    *finished = h->iteration.load() == h->props.time_steps;
+    return PLBM_OK;
+}
+
+int plbm_get_results(plbm_handler *h, int which, const double **data, size_t *count)
+{
+    if (which < 0 || which > 3) return set_err(h, Status{ PLBM_ERR_ARGUMENT, "which must be 0..3" });
+    *data = h->res_h[which];
+    *count = h->nres;
+    return PLBM_OK;
+}
+
+int plbm_get_extents(plbm_handler *h, unsigned *hn, unsigned *vn)
+{
+    *hn = h->props.horizontal_nodes;
+    *vn = h->props.vertical_nodes;
+    return PLBM_OK;
+}
+
+int plbm_get_domain(plbm_handler *h, unsigned out7[7])
+{
+    const Domain &d = h->dom;
+    const unsigned v[7] = { d.total_node_count, d.horizontal_nodes, d.vertical_nodes, d.subdomain_vertical_nodes,
+                            d.subdomain_horizontal_nodes, d.subdomain_count_vertical, d.subdomain_count_horizontal };
+    std::memcpy(out7, v, sizeof v);
+    return PLBM_OK;
+}
+
+int plbm_get_progress(plbm_handler *h, double *p) { *p = h->progress.load(); return PLBM_OK; }
+int plbm_get_last_frametime(plbm_handler *h, double *ms) { *ms = h->frametime.load(); return PLBM_OK; }
+int plbm_get_current_iteration(plbm_handler *h, unsigned *it) { *it = h->iteration.load(); return PLBM_OK; }
+
+int plbm_get_properties(plbm_handler *h, plbm_properties *out)
+{
+    *out = h->props.to_c();
+    return PLBM_OK;
+}
+
+int plbm_properties_to_json(const plbm_properties *props, const char *path)
+{
+    return guarded(nullptr, [&] {
+        const Props p = Props::make(*props);
+        props_to_json(p, props->vertical_nodes, props->horizontal_nodes, path);
+    });
+}
+
+int plbm_json_to_properties(const char *path, int offset, plbm_properties *out)
+{
+    return guarded(nullptr, [&] {
+        static thread_local Props keep;
+        keep = json_to_props(path, offset, nullptr);
+        *out = keep.to_c();
+    });
+}
+
+int plbm_run_steps(plbm_handler *h, unsigned n, double *ms_per_step)
+{
+    return guarded(h, [&] {
+        if (h->worker.joinable()) fail(PLBM_ERR_ARGUMENT, "plbm_run_steps while the step loop runs");
+        if (n == 0) return;
+        const unsigned t0 = h->iteration.load();
+        cuda_check(cudaSetDevice(h->opt.device), "cudaSetDevice");
+        if (h->opt.use_graph) h->ensure_graph();
+        cuda_check(cudaEventRecord(h->ev0, h->stream), "event");
+        h->run_plain(t0, t0 + n - 1);
+        cuda_check(h->launch_step(t0 + n - 1, true), "step");
+        cuda_check(cudaEventRecord(h->ev1, h->stream), "event");
+        cuda_check(cudaEventSynchronize(h->ev1), "steps");
+        float ms = 0;
+        cuda_check(cudaEventElapsedTime(&ms, h->ev0, h->ev1), "elapsed");
+        if (ms_per_step) *ms_per_step = ms / n;
+        h->iteration = t0 + n;
+        h->progress = (double)(t0 + n) / (double)h->props.time_steps;
+    });
+}
+
+int plbm_sync_results(plbm_handler *h)
+{
+    return guarded(h, [&] { h->copy_results(); });
+}
+
+int plbm_launches_per_step(plbm_handler *h, unsigned *n)
+{
+    (void)h;
+    *n = 1;
+    return PLBM_OK;
+}
+
+int plbm_bytes_per_node(plbm_handler *h, double *bytes)
+{
+    *bytes = 18.0 * (double)storage_bytes(h->prec);
+    return PLBM_OK;
+}
+
+int plbm_mass_momentum(plbm_handler *h, double out3[3])
+{
+    return guarded(h, [&] {
+        cuda_check(plbm::launch_reduce_results(h->res_d[0], h->res_d[1], h->res_d[2], h->flags_d, h->nres, h->red_d,
+                                               h->stream),
+                   "reduce");
+        cuda_check(cudaMemcpyAsync(out3, h->red_d, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
+        cuda_check(cudaStreamSynchronize(h->stream), "reduce");
+    });
+}
+
+const char *plbm_last_error(const plbm_handler *h)
+{
+    if (h) return h->last_error.c_str();
+    std::lock_guard<std::mutex> g(g_create_mu);
+    g_tls_error = g_create_error;
+    return g_tls_error.c_str();
+}
+
+const char *plbm_version(void) { return "portlbm_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

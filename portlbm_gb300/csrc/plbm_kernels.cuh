@@ -1,0 +1,215 @@
+// plbm_kernels.cuh — the fused per-timestep kernels.  One launch performs what the reference
+// does with EmplaceBounceBackKernel + OutletUpdateKernel + StreamCollideKernel (+ buffer
+// refreshes for the one-lattice algorithms): every fluid node gathers its nine incoming
+// populations (bounce-back and boundary values resolved at the gather), collides, and writes
+// its nine outgoing populations once.
+//
+//   nptl  two lattices, 2-D thread blocks over the inner grid            (nptl.hpp:56-141)
+//   lptl  two lattices, 1-D launch over the linear node index            (lptl.hpp:57-137)
+//   npol  one lattice, updated in place tile by tile; values crossing a tile edge are read
+//         from a double-buffered halo snapshot written by the neighbouring tile in the previous
+//         step (replaces the buffer rows/columns and their copy kernels, buffered.hpp:44-153)
+//   nsol  one lattice, in-place "AA" swap: even steps read the neighbours' opposite slots and
+//         write into the neighbours' slots, odd steps read and write the node's own slots, so
+//         every slot is read and written by one thread only (replaces the local-memory swap,
+//         nsol_kernels.hpp:171-334)
+#pragma once
+
+#include "plbm_device.cuh"
+
+namespace plbm {
+
+template <int PREC> using CT = typename Store<PREC>::C;
+
+// Incoming population d of inner node (xi, yi) for the pull schemes: ghost constant, own
+// opposite value when the source is solid, otherwise the source node's value.
+template <int PREC, int L>
+__device__ __forceinline__ CT<PREC> pull_one(const void *S, unsigned long long n, int xi, int yi, int d,
+                                             uint16_t links, const StepParams &p)
+{
+    const int sx = xi - cxd(d), sy = yi - cyd(d);
+    if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H) {
+        if (sy < 0 || sy >= p.H) return (CT<PREC>)p.weight[d];
+        return sx < 0 ? (CT<PREC>)p.feq_in[d] : (CT<PREC>)p.feq_out[d];
+    }
+    if (links & (1u << d)) return ld<PREC>(S, lidx<L>(n, 8 - d, p.N), 8 - d, p);
+    const unsigned long long s = (unsigned long long)sx + (unsigned long long)sy * p.P;
+    return ld<PREC>(S, lidx<L>(s, d, p.N), d, p);
+}
+
+template <int PREC, int L>
+__device__ __forceinline__ void update_two_lattice(int xi, int yi, const StepParams &p)
+{
+    const unsigned long long n = (unsigned long long)xi + (unsigned long long)yi * p.P;
+    const uint16_t lk = p.links[n];
+    if (!(lk & LINK_FLUID)) return;
+    CT<PREC> f[9];
+#pragma unroll
+    for (int d = 0; d < 9; ++d) f[d] = pull_one<PREC, L>(p.lat0, n, xi, yi, d, lk, p);
+    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
+    const Moments m = collide<PREC>(f, p);
+#pragma unroll
+    for (int d = 0; d < 9; ++d) st<PREC>(p.lat1, lidx<L>(n, d, p.N), d, f[d], p);
+    observables<PREC>(m, xi, yi, p);
+}
+
+// nptl: 2-D blocks (tile shape from the work-group size hint).
+template <int PREC, int L>
+__global__ void k_nptl(StepParams p)
+{
+    const int xi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int yi = blockIdx.y * blockDim.y + threadIdx.y;
+    if (xi >= p.W || yi >= p.H) return;
+    update_two_lattice<PREC, L>(xi, yi, p);
+}
+
+// lptl: 1-D launch over n = x' + y' * P (padding columns x' >= W idle).
+template <int PREC, int L>
+__global__ void k_lptl(StepParams p)
+{
+    const unsigned long long n = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= p.N) return;
+    const int yi = (int)(n / (unsigned)p.P), xi = (int)(n - (unsigned long long)yi * p.P);
+    if (xi >= p.W) return;
+    update_two_lattice<PREC, L>(xi, yi, p);
+}
+
+// ---- npol: in place, one tile per thread block --------------------------------------------
+
+// Halo snapshot layout (storage type T): columns first, then rows.
+//   col[b][y'][0..2] = dirs 2,5,8 of node (x' = (b+1)*TW - 1, y')   right edge of tile column b
+//   col[b][y'][3..5] = dirs 0,3,6 of node (x' = (b+1)*TW,     y')   left edge of tile column b+1
+//   row[b][x'][0..2] = dirs 6,7,8 of node (x', y' = (b+1)*TH - 1)   top edge of tile row b
+//   row[b][x'][3..5] = dirs 0,1,2 of node (x', y' = (b+1)*TH)       bottom edge of tile row b+1
+__device__ __forceinline__ unsigned long long halo_col(const StepParams &p, int b, int y, int k)
+{
+    return ((unsigned long long)b * p.H + y) * 6 + k;
+}
+__device__ __forceinline__ unsigned long long halo_row(const StepParams &p, int b, int x, int k)
+{
+    return (unsigned long long)p.n_col_bounds * p.H * 6 + ((unsigned long long)b * p.W + x) * 6 + k;
+}
+
+template <int PREC, int L>
+__global__ void k_npol(StepParams p)
+{
+    const int TW = p.tile_w, TH = p.tile_h;
+    const int tcx = blockIdx.x, tcy = blockIdx.y;
+    const int xi = tcx * TW + threadIdx.x, yi = tcy * TH + threadIdx.y;
+    const bool inside = xi < p.W && yi < p.H;
+    const unsigned long long n = inside ? (unsigned long long)xi + (unsigned long long)yi * p.P : 0;
+    const uint16_t lk = inside ? p.links[n] : 0;
+    const bool fluid = (lk & LINK_FLUID) != 0;
+    CT<PREC> f[9];
+    if (fluid) {
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {
+            const int sx = xi - cxd(d), sy = yi - cyd(d);
+            if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H || (lk & (1u << d)) || d == 4) {
+                f[d] = pull_one<PREC, L>(p.lat0, n, xi, yi, d, lk, p);
+            } else if (sx / TW != tcx) {
+                const int k = sx < xi ? d / 3 : 3 + d / 3;
+                const int b = sx < xi ? sx / TW : tcx;
+                f[d] = ld<PREC>(p.halo_in, halo_col(p, b, sy, k), d, p);
+            } else if (sy / TH != tcy) {
+                const int k = sy < yi ? d - 6 : 3 + d;
+                const int b = sy < yi ? sy / TH : tcy;
+                f[d] = ld<PREC>(p.halo_in, halo_row(p, b, sx, k), d, p);
+            } else {
+                const unsigned long long s = (unsigned long long)sx + (unsigned long long)sy * p.P;
+                f[d] = ld<PREC>(p.lat0, lidx<L>(s, d, p.N), d, p);
+            }
+        }
+    }
+    __syncthreads();   // every read of this tile's old values happens before any write
+    if (!fluid) return;
+    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
+    const Moments m = collide<PREC>(f, p);
+#pragma unroll
+    for (int d = 0; d < 9; ++d) st<PREC>(p.lat0, lidx<L>(n, d, p.N), d, f[d], p);
+    const int lx = threadIdx.x, ly = threadIdx.y;
+    if (lx == TW - 1 && tcx < p.n_col_bounds)
+        for (int k = 0; k < 3; ++k) st<PREC>(p.halo_out, halo_col(p, tcx, yi, k), 3 * k + 2, f[3 * k + 2], p);
+    if (lx == 0 && tcx > 0)
+        for (int k = 0; k < 3; ++k) st<PREC>(p.halo_out, halo_col(p, tcx - 1, yi, 3 + k), 3 * k, f[3 * k], p);
+    if (ly == TH - 1 && tcy < p.n_row_bounds)
+        for (int k = 0; k < 3; ++k) st<PREC>(p.halo_out, halo_row(p, tcy, xi, k), 6 + k, f[6 + k], p);
+    if (ly == 0 && tcy > 0)
+        for (int k = 0; k < 3; ++k) st<PREC>(p.halo_out, halo_row(p, tcy - 1, xi, 3 + k), k, f[k], p);
+    observables<PREC>(m, xi, yi, p);
+}
+
+// ---- nsol: in-place AA swap ---------------------------------------------------------------
+// Slot (m, k) denotes lattice entry lidx(m, k).  Between steps the lattice alternates between
+//   state P (before an even step): slot (m, 8-k) holds node m's post-collision value of k;
+//   state Q (before an odd step):  slot (m, k) holds the value arriving at m along k.
+// The initial rest state is both (weights are symmetric, w_k = w_{8-k}).
+
+template <int PREC, int L>
+__global__ void k_nsol_even(StepParams p)
+{
+    const int xi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int yi = blockIdx.y * blockDim.y + threadIdx.y;
+    if (xi >= p.W || yi >= p.H) return;
+    const unsigned long long n = (unsigned long long)xi + (unsigned long long)yi * p.P;
+    const uint16_t lk = p.links[n];
+    if (!(lk & LINK_FLUID)) return;
+    CT<PREC> f[9];
+#pragma unroll
+    for (int d = 0; d < 9; ++d) {
+        const int sx = xi - cxd(d), sy = yi - cyd(d);
+        if (d == 4) {
+            f[4] = ld<PREC>(p.lat0, lidx<L>(n, 4, p.N), 4, p);
+        } else if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H) {
+            f[d] = (sy < 0 || sy >= p.H) ? (CT<PREC>)p.weight[d] : (sx < 0 ? (CT<PREC>)p.feq_in[d] : (CT<PREC>)p.feq_out[d]);
+        } else if (lk & (1u << d)) {
+            f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N), d, p);          // own post-collision 8-d
+        } else {
+            const unsigned long long s = (unsigned long long)sx + (unsigned long long)sy * p.P;
+            f[d] = ld<PREC>(p.lat0, lidx<L>(s, 8 - d, p.N), 8 - d, p);
+        }
+    }
+    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
+    const Moments m = collide<PREC>(f, p);
+#pragma unroll
+    for (int d = 0; d < 9; ++d) {
+        const int tx = xi + cxd(d), ty = yi + cyd(d);
+        if (tx < 0 || tx >= p.W || ty < 0 || ty >= p.H) continue;   // toward a ghost: never read
+        const unsigned long long t = (unsigned long long)tx + (unsigned long long)ty * p.P;
+        st<PREC>(p.lat0, lidx<L>(t, d, p.N), d, f[d], p);
+    }
+    observables<PREC>(m, xi, yi, p);
+}
+
+template <int PREC, int L>
+__global__ void k_nsol_odd(StepParams p)
+{
+    const int xi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int yi = blockIdx.y * blockDim.y + threadIdx.y;
+    if (xi >= p.W || yi >= p.H) return;
+    const unsigned long long n = (unsigned long long)xi + (unsigned long long)yi * p.P;
+    const uint16_t lk = p.links[n];
+    if (!(lk & LINK_FLUID)) return;
+    CT<PREC> f[9];
+#pragma unroll
+    for (int d = 0; d < 9; ++d) {
+        const int sx = xi - cxd(d), sy = yi - cyd(d);
+        if (d == 4) {
+            f[4] = ld<PREC>(p.lat0, lidx<L>(n, 4, p.N), 4, p);
+        } else if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H) {
+            f[d] = (sy < 0 || sy >= p.H) ? (CT<PREC>)p.weight[d] : (sx < 0 ? (CT<PREC>)p.feq_in[d] : (CT<PREC>)p.feq_out[d]);
+        } else if (lk & (1u << d)) {
+            const unsigned long long s = (unsigned long long)sx + (unsigned long long)sy * p.P;
+            f[d] = ld<PREC>(p.lat0, lidx<L>(s, 8 - d, p.N), 8 - d, p);  // parked in the solid's slot
+        } else {
+            f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N), d, p);
+        }
+    }
+    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
+    const Moments m = collide<PREC>(f, p);
+#pragma unroll
+    for (int d = 0; d < 9; ++d) st<PREC>(p.lat0, lidx<L>(n, 8 - d, p.N), 8 - d, f[d], p);
+    observables<PREC>(m, xi, yi, p);
+}
+
+}  // namespace plbm

@@ -1,0 +1,26 @@
+// plbm_launch.h — host-visible launch entry points of the device code.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "plbm_params.h"
+
+namespace plbm {
+
+// One timestep of algorithm `alg` (0 nptl, 1 lptl, 2 npol, 3 nsol) for precision `prec` and
+// layout `lay`; `t` is the absolute step index (selects the nsol parity kernel).
+cudaError_t launch_nptl(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s);
+cudaError_t launch_lptl(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s);
+cudaError_t launch_npol(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s);
+cudaError_t launch_nsol(int prec, int lay, const StepParams &p, unsigned t, dim3 grid, dim3 block, cudaStream_t s);
+
+// Set-up kernels (plbm_util.cu).
+cudaError_t launch_links(const int8_t *flags, uint16_t *links, int W, int H, int P, cudaStream_t s);
+cudaError_t launch_fill_lattice(void *lat, int prec, int lay, unsigned long long N, const double w[9], cudaStream_t s);
+cudaError_t launch_fill_halo(void *halo, int prec, int W, int H, int ncb, int nrb, const double w[9], cudaStream_t s);
+cudaError_t launch_fill_results(double *rho, double *jx, double *jy, double *ja, unsigned long long n, cudaStream_t s);
+// FP64 sums over fluid nodes of the result arrays: out3 = {sum rho, sum jx, sum jy}.
+cudaError_t launch_reduce_results(const double *rho, const double *jx, const double *jy, const int8_t *flags,
+                                  unsigned long long n, double *out3_dev, cudaStream_t s);
+int max_threads_for(int alg, int prec, int lay);
+
+}  // namespace plbm

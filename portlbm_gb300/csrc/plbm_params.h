@@ -1,0 +1,34 @@
+// plbm_params.h — step parameters shared by host and device code (host-safe header).
+#pragma once
+
+#include <stdint.h>
+
+namespace plbm {
+
+enum Layout { COLLISION = 0, STREAM = 1, BUNDLE = 2 };
+enum Precision { F64_STRICT = 0, F64_FAST = 1, F32_REF = 2, F32 = 3, F16S = 4, BF16S = 5 };
+
+constexpr uint16_t LINK_FLUID = 1u << 4;
+
+// Step parameters, passed by value to every step kernel.
+struct StepParams {
+    void *lat0;                 // source lattice (two-lattice) / the lattice (one-lattice)
+    void *lat1;                 // destination lattice (two-lattice only)
+    const uint16_t *links;      // per node: bit d (d != 4) pull source solid, bit 4 fluid
+    double *rho, *jx, *jy, *jabs;   // results, W*H doubles, row-major over the inner domain
+    const double *jy_prev;      // jy of the previous step at x' = W-2 (H entries)
+    double *jy_next;            // jy of this step at x' = W-2
+    double *halo_in, *halo_out; // one-lattice tile halos (npol) [cols | rows]
+    int W, H, P;
+    unsigned long long N;
+    int tile_w, tile_h;         // npol tile
+    int n_col_bounds, n_row_bounds;
+    double omega;               // 1 / relaxation_time, in the storage precision's value
+    double rho_out;
+    double feq_in[9], feq_out[9], weight[9];   // ghost constants in the policy's arithmetic
+    int outlet_mode;            // 0: Zou/He-type density outlet; 1: constant feq(outlet) ghost
+    int nan_protection;
+    int write_results;          // this step is copied to the host
+};
+
+}  // namespace plbm

@@ -1,0 +1,159 @@
+// plbm_util.cu — set-up and reduction kernels: link masks, lattice/halo/result fills, and the
+// FP64 mass/momentum reduction.
+#include "plbm_device.cuh"
+#include "plbm_launch.h"
+
+namespace plbm {
+
+// Packs, for every inner node, whether it is fluid (bit 4) and which pull sources n - c_d are
+// solid (bit d).  flags: W*H int8 (0 fluid, 1 solid), row-major; links: P*H uint16.
+__global__ void k_links(const int8_t *flags, uint16_t *links, int W, int H, int P)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= P || y >= H) return;
+    uint16_t v = 0;
+    if (x < W && flags[(size_t)y * W + x] == 0) {
+        v = LINK_FLUID;
+        for (int d = 0; d < 9; ++d) {
+            if (d == 4) continue;
+            const int sx = x - (d % 3 - 1), sy = y - (d / 3 - 1);
+            if (sx < 0 || sx >= W || sy < 0 || sy >= H) continue;
+            if (flags[(size_t)sy * W + sx] == 1) v |= (uint16_t)(1u << d);
+        }
+    }
+    links[(size_t)y * P + x] = v;
+}
+
+cudaError_t launch_links(const int8_t *flags, uint16_t *links, int W, int H, int P, cudaStream_t s)
+{
+    dim3 grid((P + 255) / 256, H);
+    k_links<<<grid, 256, 0, s>>>(flags, links, W, H, P);
+    return cudaGetLastError();
+}
+
+struct W9 { double w[9]; };
+
+template <int PREC>
+__global__ void k_fill_lattice(void *lat, int lay, unsigned long long N, W9 w)
+{
+    using T = typename Store<PREC>::T;
+    const unsigned long long total = 9ull * N;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        int d;
+        if (lay == COLLISION) d = (int)(i % 9);
+        else if (lay == STREAM) d = (int)(i / N);
+        else d = 3 * (int)(i / (3 * N)) + (int)((i % (3 * N)) % 3);
+        T *b = static_cast<T *>(lat);
+        if constexpr (PREC == F16S) b[i] = __float2half_rn(0.0f);
+        else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(0.0f);
+        else b[i] = (T)w.w[d];
+    }
+}
+
+cudaError_t launch_fill_lattice(void *lat, int prec, int lay, unsigned long long N, const double w[9], cudaStream_t s)
+{
+    W9 ww;
+    for (int i = 0; i < 9; ++i) ww.w[i] = w[i];
+    const int grid = 152 * 8, block = 256;
+    switch (prec) {
+    case F64_STRICT: case F64_FAST: k_fill_lattice<F64_STRICT><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
+    case F32_REF: case F32: k_fill_lattice<F32><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
+    case F16S: k_fill_lattice<F16S><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
+    case BF16S: k_fill_lattice<BF16S><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// Halo snapshot entries hold the rest state initially; the direction of each slot follows the
+// layout documented at k_npol.
+template <int PREC>
+__global__ void k_fill_halo(void *halo, unsigned long long ncol, unsigned long long total, W9 w)
+{
+    using T = typename Store<PREC>::T;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const int k = (int)(i % 6);
+        int d;
+        if (i < ncol) d = k < 3 ? 3 * k + 2 : 3 * (k - 3);
+        else d = k < 3 ? 6 + k : k - 3;
+        T *b = static_cast<T *>(halo);
+        if constexpr (PREC == F16S) b[i] = __float2half_rn(0.0f);
+        else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(0.0f);
+        else b[i] = (T)w.w[d];
+    }
+}
+
+cudaError_t launch_fill_halo(void *halo, int prec, int W, int H, int ncb, int nrb, const double w[9], cudaStream_t s)
+{
+    W9 ww;
+    for (int i = 0; i < 9; ++i) ww.w[i] = w[i];
+    const unsigned long long ncol = (unsigned long long)ncb * H * 6, total = ncol + (unsigned long long)nrb * W * 6;
+    if (total == 0) return cudaSuccess;
+    const int grid = 152 * 2, block = 256;
+    switch (prec) {
+    case F64_STRICT: case F64_FAST: k_fill_halo<F64_STRICT><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
+    case F32_REF: case F32: k_fill_halo<F32><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
+    case F16S: k_fill_halo<F16S><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
+    case BF16S: k_fill_halo<BF16S><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// core::Results starts as if every node were solid: rho = -1, j = 0 (simulation.cpp:386-417).
+__global__ void k_fill_results(double *rho, double *jx, double *jy, double *ja, unsigned long long n)
+{
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        rho[i] = -1.0; jx[i] = 0.0; jy[i] = 0.0; ja[i] = 0.0;
+    }
+}
+
+cudaError_t launch_fill_results(double *rho, double *jx, double *jy, double *ja, unsigned long long n, cudaStream_t s)
+{
+    k_fill_results<<<152 * 4, 256, 0, s>>>(rho, jx, jy, ja, n);
+    return cudaGetLastError();
+}
+
+// Block-wise FP64 sums, then one atomicAdd per block and quantity.
+__global__ void k_reduce_results(const double *rho, const double *jx, const double *jy, const int8_t *flags,
+                                 unsigned long long n, double *out)
+{
+    double a = 0, b = 0, c = 0;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        if (flags[i] == 0) { a += rho[i]; b += jx[i]; c += jy[i]; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    __shared__ double sm[3][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { sm[0][wid] = a; sm[1][wid] = b; sm[2][wid] = c; }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        a = lane < nw ? sm[0][lane] : 0; b = lane < nw ? sm[1][lane] : 0; c = lane < nw ? sm[2][lane] : 0;
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            b += __shfl_down_sync(0xffffffffu, b, o);
+            c += __shfl_down_sync(0xffffffffu, c, o);
+        }
+        if (lane == 0) { atomicAdd(&out[0], a); atomicAdd(&out[1], b); atomicAdd(&out[2], c); }
+    }
+}
+
+cudaError_t launch_reduce_results(const double *rho, const double *jx, const double *jy, const int8_t *flags,
+                                  unsigned long long n, double *out3, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(out3, 0, 3 * sizeof(double), s);
+    if (e != cudaSuccess) return e;
+    k_reduce_results<<<152 * 2, 256, 0, s>>>(rho, jx, jy, flags, n, out3);
+    return cudaGetLastError();
+}
+
+}  // namespace plbm

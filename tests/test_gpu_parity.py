@@ -1,0 +1,76 @@
+"""Parity of the CUDA path with the CPU oracle (restated reference), through the C ABI.
+
+The drop-in form (f64_strict) must match the oracle exactly (max-abs difference 0.0) for
+every algorithm x data layout; f64_fast must agree within 1e-12 (the tolerance of the
+reference comparison); the buffered-outlet case (W-1 divisible by the subdomain width,
+src/lbm/core/simulation.cpp + include/lbm/gpu/general/buffered.hpp:285-288) must reproduce the
+reference's npol/nsol behaviour.
+"""
+import numpy as np
+import pytest
+
+ALGS = ["nptl", "lptl", "npol", "nsol"]
+LAYOUTS = ["collision", "stream", "bundle"]
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(plbm, alg, lay, scenario, w, h, steps, wg=64, precision="f64_strict", rho_in=1.05, tau=0.6, mask=None,
+            fui=None):
+    props = plbm.Properties(alg, lay, False, wg, steps, fui or steps, scenario, h, w, 0.0, 0.0, rho_in, 0.0, 0.0,
+                            1.0, tau)
+    hd = plbm.create_handler(props, precision=precision, mask=mask)
+    hd.start()
+    hd.block_until_finished()
+    out = {"rho": hd.get_densities(), "jx": hd.get_x_velocities(), "jy": hd.get_y_velocities(),
+           "jabs": hd.get_absolute_velocities()}
+    hd.close()
+    return out
+
+
+def run_oracle(oracle_mod, alg, lay, scenario, w, h, steps, wg=64, rho_in=1.05, tau=0.6, mask=None):
+    o = oracle_mod.Oracle(alg, lay, wg, scenario, w, h, inlet_density=rho_in, relaxation_time=tau, mask=mask)
+    o.run(steps)
+    return o.results()
+
+
+def maxdiff(a, b):
+    return max(float(np.max(np.abs(a[k] - b[k]))) for k in a)
+
+
+@pytest.mark.parametrize("alg", ALGS)
+@pytest.mark.parametrize("lay", LAYOUTS)
+def test_strict_matches_oracle_exactly(plbm, oracle_mod, alg, lay):
+    ref = run_oracle(oracle_mod, alg, lay, "circle", 62, 30, 300)
+    got = run_gpu(plbm, alg, lay, "circle", 62, 30, 300)
+    assert maxdiff(got, ref) == 0.0
+
+
+@pytest.mark.parametrize("alg", ALGS)
+def test_fast_within_tolerance(plbm, oracle_mod, alg):
+    ref = run_oracle(oracle_mod, alg, "stream", "circle", 62, 30, 300)
+    got = run_gpu(plbm, alg, "stream", "circle", 62, 30, 300, precision="f64_fast")
+    assert maxdiff(got, ref) <= 1e-12
+
+
+@pytest.mark.parametrize("alg,w,wg", [("npol", 65, 64), ("nsol", 61, 64), ("npol", 33, 16), ("nsol", 33, 16)])
+def test_buffered_outlet_case(plbm, oracle_mod, alg, w, wg):
+    ref = run_oracle(oracle_mod, alg, "stream", "Hagen-Poiseuille", w, 20, 300, wg=wg)
+    got = run_gpu(plbm, alg, "stream", "Hagen-Poiseuille", w, 20, 300, wg=wg)
+    assert maxdiff(got, ref) == 0.0
+
+
+@pytest.mark.parametrize("scenario", ["walls", "square", "plate", "skyscraper", "wing"])
+def test_scenarios_exact(plbm, oracle_mod, scenario):
+    ref = run_oracle(oracle_mod, "nptl", "stream", scenario, 90, 48, 200)
+    got = run_gpu(plbm, "nptl", "stream", scenario, 90, 48, 200)
+    assert maxdiff(got, ref) == 0.0
+
+
+def test_poiseuille_config_exact_10k_steps(plbm, oracle_mod):
+    """Config: Hagen-Poiseuille 400x100, nptl + stream, tau 0.6, rho 1.2/1.0, 10^4 steps."""
+    ref = run_oracle(oracle_mod, "nptl", "stream", "Hagen-Poiseuille", 400, 100, 10000, wg=1024, rho_in=1.2)
+    got = run_gpu(plbm, "nptl", "stream", "Hagen-Poiseuille", 400, 100, 10000, wg=1024, rho_in=1.2)
+    assert maxdiff(got, ref) == 0.0
+    fast = run_gpu(plbm, "nptl", "stream", "Hagen-Poiseuille", 400, 100, 10000, wg=1024, rho_in=1.2,
+                   precision="f64_fast")
+    assert maxdiff(fast, ref) <= 1e-12
