@@ -1,0 +1,333 @@
+"""Benchmark of PortLBM's per-timestep D2Q9 BGK update on GB300 (one JSON line on stdout).
+
+Workload: the FP64 drop-in at 8192 x 8192 inner nodes — channel with bounce-back walls, a circle
+obstacle of radius H/8 centred at (W/4, H/2), inlet density 1.2 / outlet 1.0, tau 0.6, nptl
+algorithm, stream layout.  A "step" is one lattice-Boltzmann timestep over the whole domain.
+
+* ``value``      MLUPS (W*H inner nodes x steps / s) of K device-resident steps, timed with CUDA
+                 events on the solver's stream; FP64 "fast" form (FMA-regrouped BGK, agrees with
+                 the reference to <= 1e-12, see tests/test_gpu_parity.py).
+* ``e2e``        the same metric through the public API with host buffers: create_handler from
+                 host properties + host mask (H2D), K steps, results read back (D2H), all timed.
+* ``roofline``   HBM roofline of the step kernel: 144 algorithmic bytes per node update (9 loads +
+                 9 stores of 8 B) / CUDA-event time per launch, against MEASURED_PEAKS.json.
+* ``cpu_baseline`` the CPU oracle (restated reference, OpenMP over all host cores) on a bounded
+                 sample of the same workload.
+* ``--impl reference`` times the CPU oracle as the reference arm (the reference's own SYCL build
+                 needs AdaptiveCpp/LLVM, absent here and on the GPU host).
+
+Multi-GPU: the path does not shard (no halo exchange is implemented); N ranks run N independent
+replicas ("scaling": "weak") and `value` sums them.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W_DEFAULT, H_DEFAULT = 8192, 8192
+BYTES_PER_NODE = {"f64_strict": 144.0, "f64_fast": 144.0, "f32_ref": 72.0, "f32": 72.0, "f16s": 36.0, "bf16s": 36.0}
+
+
+def circle_channel_mask(w: int, h: int) -> np.ndarray:
+    """Walls on the first/last inner row and a disk of radius floor(H/8) at (floor(W/4), floor(H/2))
+    (inner coordinates, 0-based)."""
+    yy, xx = np.mgrid[0:h, 0:w]
+    r = h // 8
+    m = ((xx - w // 4) ** 2 + (yy - h // 2) ** 2 <= r * r).astype(np.int8)
+    m[0, :] = 1
+    m[h - 1, :] = 1
+    return m
+
+
+def peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = max(smax, float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_props(plbm, alg, lay, w, h, steps, fui=None, wg=1024):
+    return plbm.Properties(alg, lay, False, wg, steps, fui or steps, "Hagen-Poiseuille", h, w, 0.0, 0.0, 1.2, 0.0,
+                           0.0, 1.0, 0.6)
+
+
+def device_run(plbm, precision, alg, lay, w, h, mask, steps, warmup):
+    """K device-resident steps; returns (ms_per_step, handler)."""
+    hd = plbm.create_handler(make_props(plbm, alg, lay, w, h, steps + warmup + 10), precision=precision, mask=mask)
+    hd.run_steps(warmup)
+    ms = hd.run_steps(steps)
+    return ms, hd
+
+
+def e2e_run(plbm, precision, alg, lay, w, h, mask, steps):
+    """Public API, host buffers in and out: create (H2D mask), K steps, results D2H."""
+    import torch
+    pinned = torch.from_numpy(mask.reshape(-1)).pin_memory().numpy()
+    t0 = time.perf_counter()
+    hd = plbm.create_handler(make_props(plbm, alg, lay, w, h, steps), precision=precision, mask=pinned.reshape(h, w))
+    hd.start()
+    hd.block_until_finished()
+    outs = [hd.get_densities(copy=False), hd.get_x_velocities(copy=False), hd.get_y_velocities(copy=False),
+            hd.get_absolute_velocities(copy=False)]
+    checksum = float(sum(float(o[:: max(1, o.size // 4096)].sum()) for o in outs))
+    t1 = time.perf_counter()
+    hd.close()
+    return (t1 - t0) * 1e3, checksum
+
+
+def cpu_oracle_sample(w, h, steps, mask, threads=None):
+    """Times the CPU oracle (all OpenMP threads) on `steps` timesteps of the same workload."""
+    from oracle import plbm_oracle
+    plbm_oracle.build()
+    o = plbm_oracle.Oracle("nptl", "stream", 1024, "Hagen-Poiseuille", w, h, inlet_density=1.2,
+                           relaxation_time=0.6, mask=mask)
+    o.run(1)
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    return w * h * steps / dt / 1e6, plbm_oracle.threads(), dt
+
+
+def load_traffic(kind: str):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(kind)
+    except Exception:
+        return None
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def max_over_ranks(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the CPU oracle on the host cores, rank 0 only."""
+    if rank != 0:
+        return
+    w, h = args.width, args.height
+    mask = circle_channel_mask(w, h)
+    per_step = []
+    from oracle import plbm_oracle
+    plbm_oracle.build()
+    o = plbm_oracle.Oracle("nptl", "stream", 1024, "Hagen-Poiseuille", w, h, inlet_density=1.2, relaxation_time=0.6,
+                           mask=mask)
+    for _ in range(args.warmup):
+        o.run(1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        o.run(1)
+        per_step.append(time.perf_counter() - t)
+    dt = time.perf_counter() - t0
+    mlups = w * h * args.steps / dt / 1e6
+    line = {"metric": "MLUPS (FP64 D2Q9 BGK, 8192x8192 circle channel)", "value": round(mlups, 2), "unit": "MLUPS",
+            "impl": "reference", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * dt / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"circle channel {w}x{h}, nptl+stream, tau 0.6, rho 1.2/1.0", "algorithm": "nptl",
+                       "data_layout": "stream", "precision": "f64"},
+            "cpu_baseline": {"value": round(mlups, 2), "unit": "MLUPS", "cores": plbm_oracle.threads(),
+                             "kind": "port",
+                             "sample": f"{args.steps} full {w}x{h} timesteps of the CPU oracle (restated reference, "
+                                       "OpenMP) after warm-up"},
+            "e2e": {"value": round(mlups, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--width", type=int, default=W_DEFAULT)
+    ap.add_argument("--height", type=int, default=H_DEFAULT)
+    ap.add_argument("--precision", default="f64_fast", choices=list(BYTES_PER_NODE))
+    ap.add_argument("--algorithm", default="nptl")
+    ap.add_argument("--layout", default="stream")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=0, help="CPU-baseline sample steps (0: auto)")
+    ap.add_argument("--kernel-only", action="store_true", help="only the device-resident timed region (profiling)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import portlbm_gb300 as plbm
+    from portlbm_gb300 import build as b
+    b.build()
+    w, h = args.width, args.height
+    mask = circle_channel_mask(w, h)
+    pk = peaks()
+
+    # -- device-resident timed region (value + roofline) --
+    barrier(world)
+    with ClockSampler(local) as clocks:
+        ms, hd = device_run(plbm, args.precision, args.algorithm, args.layout, w, h, mask, args.steps, args.warmup)
+    barrier(world)
+    ms = max_over_ranks(ms, world)
+    launches = hd.launches_per_step() * args.steps
+    bpn = BYTES_PER_NODE[args.precision]
+    mlups_rank = w * h / (ms * 1e-3) / 1e6
+    value = mlups_rank * world
+    achieved_gbs = bpn * w * h / (ms * 1e-3) / 1e9
+    hd.close()
+
+    if args.kernel_only:
+        if rank == 0:
+            print(json.dumps({"value": round(value, 1), "unit": "MLUPS", "ms_per_step": round(ms, 4),
+                              "achieved_gbs": round(achieved_gbs, 1), "precision": args.precision}), flush=True)
+        return
+
+    # -- end-to-end through the public API with host buffers --
+    e2e_steps = args.steps
+    e2e_ms, _ = e2e_run(plbm, args.precision, args.algorithm, args.layout, w, h, mask, e2e_steps)
+    e2e_ms = max_over_ranks(e2e_ms, world)
+    e2e_mlups = world * w * h * e2e_steps / (e2e_ms * 1e-3) / 1e6
+
+    # -- other forms of the same step (device-resident, same K), reported beside --
+    variants = {}
+    if not args.no_variants and rank == 0:
+        for prec in ("f64_strict", "f32", "f16s", "bf16s"):
+            if prec == args.precision:
+                continue
+            vms, vh = device_run(plbm, prec, args.algorithm, args.layout, w, h, mask, max(20, args.steps // 4), 5)
+            vh.close()
+            variants[prec] = {"mlups": round(w * h / vms / 1e3, 1), "ms_per_step": round(vms, 4),
+                              "hbm_gbs": round(BYTES_PER_NODE[prec] * w * h / vms / 1e6, 1),
+                              "frac_of_hbm": round(BYTES_PER_NODE[prec] * w * h / vms / 1e6 / pk["hbm_gbs"], 4)}
+
+    # -- CPU baseline (rank 0, N = 1) --
+    cpu = None
+    if rank == 0 and world == 1:
+        steps = args.cpu_steps or 20
+        v, cores, dt = cpu_oracle_sample(w, h, steps, mask)
+        cpu = {"value": round(v, 2), "unit": "MLUPS", "cores": cores, "kind": "port",
+               "sample": f"{steps} full {w}x{h} timesteps of the CPU oracle (restated reference, OpenMP, "
+                         f"{dt:.1f} s)"}
+
+    if rank == 0:
+        traffic = load_traffic(f"{args.algorithm}_{args.layout}_{args.precision}")
+        line = {
+            "metric": "MLUPS (FP64 D2Q9 BGK, 8192x8192 circle channel)",
+            "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"circle channel {w}x{h} (r=H/8 at W/4), nptl+stream, tau 0.6, rho 1.2/1.0",
+                       "algorithm": args.algorithm, "data_layout": args.layout, "precision": args.precision,
+                       "l2": "inputs larger than L2 (lattice %.1f GB)" % (2 * 9 * 8 * w * h / 1e9),
+                       "parallelism": f"replicas{world}"},
+            "roofline": {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": round(achieved_gbs / pk["hbm_gbs"], 4), "traffic": traffic,
+                         "peak_source": pk["source"],
+                         "note": "FP64 forms issue-bound on the FP64 pipe (0.5 T DP instr/s measured)"},
+            "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS", "h2d_bytes_per_step": round(w * h / e2e_steps),
+                    "d2h_bytes_per_step": round(4 * 8 * w * h / e2e_steps)},
+            "gpu_launches": launches,
+            "clocks": clocks.summary(),
+            "cpu_baseline": cpu,
+            "variants": variants,
+        }
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

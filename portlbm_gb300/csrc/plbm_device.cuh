@@ -58,8 +58,8 @@ __device__ __forceinline__ typename Store<PREC>::C ld(const void *base, unsigned
 {
     using T = typename Store<PREC>::T;
     const T *b = static_cast<const T *>(base);
-    if constexpr (PREC == F16S) return __half2float(b[i]) + (float)p.weight[d];
-    else if constexpr (PREC == BF16S) return __bfloat162float(b[i]) + (float)p.weight[d];
+    if constexpr (PREC == F16S) return __half2float(b[i]) + p.weightf[d];
+    else if constexpr (PREC == BF16S) return __bfloat162float(b[i]) + p.weightf[d];
     else return b[i];
 }
 
@@ -68,8 +68,8 @@ __device__ __forceinline__ void st(void *base, unsigned long long i, int d, type
 {
     using T = typename Store<PREC>::T;
     T *b = static_cast<T *>(base);
-    if constexpr (PREC == F16S) b[i] = __float2half_rn(v - (float)p.weight[d]);
-    else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(v - (float)p.weight[d]);
+    if constexpr (PREC == F16S) b[i] = __float2half_rn(v - p.weightf[d]);
+    else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(v - p.weightf[d]);
     else b[i] = v;
 }
 
@@ -236,8 +236,8 @@ __device__ __forceinline__ Moments collide(typename Store<PREC>::C f[9], const S
 {
     if constexpr (PREC == F64_STRICT) return collide_f64_strict(f, p.omega);
     else if constexpr (PREC == F64_FAST) return collide_f64_fast(f, p.omega);
-    else if constexpr (PREC == F32_REF) return collide_f32_ref(f, (float)p.omega);
-    else return collide_f32(f, (float)p.omega);
+    else if constexpr (PREC == F32_REF) return collide_f32_ref(f, p.omegaf);
+    else return collide_f32(f, p.omegaf);
 }
 
 // Outlet populations 0, 3, 6 of a border node (X-2, y), y in [2, V-3], from its other pulled
@@ -257,7 +257,7 @@ __device__ __forceinline__ void outlet_fill(typename Store<PREC>::C f[9], double
         f[3] = __dsub_rn(g1, __dmul_rn(2.0 / 3, xv));
         f[6] = __dadd_rn(__dsub_rn(__dadd_rn(g2, hd), x6), hy);
     } else if constexpr (PREC == F32_REF) {
-        const float xv = __fadd_rn(-(float)p.rho_out,
+        const float xv = __fadd_rn(-p.rho_outf,
                                    __fadd_rn(__fadd_rn(__fadd_rn(f[1], f[4]), f[7]),
                                              __fmul_rn(2.0f, __fadd_rn(__fadd_rn(f[8], f[5]), f[2]))));
         const double hd = __dmul_rn(0.5, (double)__fsub_rn(f[1], f[7]));
@@ -268,7 +268,7 @@ __device__ __forceinline__ void outlet_fill(typename Store<PREC>::C f[9], double
         f[6] = (float)__dadd_rn(__dsub_rn(__dadd_rn((double)g2, hd), x6), hy);
     } else {
         using C = typename Store<PREC>::C;
-        const C xv = -(C)p.rho_out + ((f[1] + f[4] + f[7]) + (C)2 * (f[8] + f[5] + f[2]));
+        const C xv = -p.rho_outf + ((f[1] + f[4] + f[7]) + (C)2 * (f[8] + f[5] + f[2]));
         const C hd = (C)0.5 * (f[1] - f[7]), x6 = xv * (C)(1.0 / 6), hy = (C)(0.5 * jyo);
         const C g0 = f[8], g1 = f[5], g2 = f[2];
         f[0] = g0 - hd - x6 - hy;
@@ -277,15 +277,19 @@ __device__ __forceinline__ void outlet_fill(typename Store<PREC>::C f[9], double
     }
 }
 
-// Value of ghost node (sx, sy) (reference coordinates) in direction d.
-template <typename C>
-__device__ __forceinline__ C ghost_value(int sx, int sy, int d, const StepParams &p)
+// Ghost constants in the compute type: rest weights (bottom/top ghost rows), feq(inlet)
+// (x = 0), feq(outlet) (x = X-1).
+template <int PREC> __device__ __forceinline__ typename Store<PREC>::C g_weight(const StepParams &p, int d)
 {
-    const int X = p.W + 2, V = p.H + 2;
-    if (sy <= 0 || sy >= V - 1) return (C)p.weight[d];
-    if (sx <= 0) return (C)p.feq_in[d];
-    (void)X;
-    return (C)p.feq_out[d];
+    if constexpr (sizeof(typename Store<PREC>::C) == 8) return p.weight[d]; else return p.weightf[d];
+}
+template <int PREC> __device__ __forceinline__ typename Store<PREC>::C g_in(const StepParams &p, int d)
+{
+    if constexpr (sizeof(typename Store<PREC>::C) == 8) return p.feq_in[d]; else return p.feq_inf[d];
+}
+template <int PREC> __device__ __forceinline__ typename Store<PREC>::C g_out(const StepParams &p, int d)
+{
+    if constexpr (sizeof(typename Store<PREC>::C) == 8) return p.feq_out[d]; else return p.feq_outf[d];
 }
 
 // Writes the macroscopic observables of node (x', y') when this step is copied to the host,

@@ -567,6 +567,13 @@ struct plbm_handler {
             b.omega = (double)(1 / (float)props.tau);
             b.rho_out = (double)(float)props.orho;
         }
+        for (int d = 0; d < 9; ++d) {
+            b.weightf[d] = (float)b.weight[d];
+            b.feq_inf[d] = (float)b.feq_in[d];
+            b.feq_outf[d] = (float)b.feq_out[d];
+        }
+        b.omegaf = (float)b.omega;
+        b.rho_outf = (float)b.rho_out;
         for (int i = 0; i < (two_lattice() ? 2 : 1); ++i)
             cuda_check(plbm::launch_fill_lattice(lat[i], prec, lay, N, b.weight, stream), "lattice fill");
 

@@ -29,8 +29,8 @@ __device__ __forceinline__ CT<PREC> pull_one(const void *S, unsigned long long n
 {
     const int sx = xi - cxd(d), sy = yi - cyd(d);
     if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H) {
-        if (sy < 0 || sy >= p.H) return (CT<PREC>)p.weight[d];
-        return sx < 0 ? (CT<PREC>)p.feq_in[d] : (CT<PREC>)p.feq_out[d];
+        if (sy < 0 || sy >= p.H) return g_weight<PREC>(p, d);
+        return sx < 0 ? g_in<PREC>(p, d) : g_out<PREC>(p, d);
     }
     if (links & (1u << d)) return ld<PREC>(S, lidx<L>(n, 8 - d, p.N), 8 - d, p);
     const unsigned long long s = (unsigned long long)sx + (unsigned long long)sy * p.P;
@@ -161,7 +161,7 @@ __global__ void k_nsol_even(StepParams p)
         if (d == 4) {
             f[4] = ld<PREC>(p.lat0, lidx<L>(n, 4, p.N), 4, p);
         } else if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H) {
-            f[d] = (sy < 0 || sy >= p.H) ? (CT<PREC>)p.weight[d] : (sx < 0 ? (CT<PREC>)p.feq_in[d] : (CT<PREC>)p.feq_out[d]);
+            f[d] = (sy < 0 || sy >= p.H) ? g_weight<PREC>(p, d) : (sx < 0 ? g_in<PREC>(p, d) : g_out<PREC>(p, d));
         } else if (lk & (1u << d)) {
             f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N), d, p);          // own post-collision 8-d
         } else {
@@ -197,7 +197,7 @@ __global__ void k_nsol_odd(StepParams p)
         if (d == 4) {
             f[4] = ld<PREC>(p.lat0, lidx<L>(n, 4, p.N), 4, p);
         } else if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H) {
-            f[d] = (sy < 0 || sy >= p.H) ? (CT<PREC>)p.weight[d] : (sx < 0 ? (CT<PREC>)p.feq_in[d] : (CT<PREC>)p.feq_out[d]);
+            f[d] = (sy < 0 || sy >= p.H) ? g_weight<PREC>(p, d) : (sx < 0 ? g_in<PREC>(p, d) : g_out<PREC>(p, d));
         } else if (lk & (1u << d)) {
             const unsigned long long s = (unsigned long long)sx + (unsigned long long)sy * p.P;
             f[d] = ld<PREC>(p.lat0, lidx<L>(s, 8 - d, p.N), 8 - d, p);  // parked in the solid's slot

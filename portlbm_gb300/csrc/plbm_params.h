@@ -26,6 +26,10 @@ struct StepParams {
     double omega;               // 1 / relaxation_time, in the storage precision's value
     double rho_out;
     double feq_in[9], feq_out[9], weight[9];   // ghost constants in the policy's arithmetic
+    // float copies for the FP32-arithmetic forms (a double->float conversion in the inner loop
+    // would run on the FP64 pipe)
+    float feq_inf[9], feq_outf[9], weightf[9];
+    float omegaf, rho_outf;
     int outlet_mode;            // 0: Zou/He-type density outlet; 1: constant feq(outlet) ghost
     int nan_protection;
     int write_results;          // this step is copied to the host
