@@ -140,6 +140,44 @@ int plbm_bytes_per_node(plbm_handler *h, double *bytes);
 /* Reads back the total fluid mass and momentum (FP64 reductions on the GPU). */
 int plbm_mass_momentum(plbm_handler *h, double out3[3]);
 
+/* ---- no-allocation entry point (no counterpart in the reference) ----------------------------
+ * plbm_nptl_steps_noalloc runs `steps` timesteps of the nptl step kernel (FP64 drop-in form,
+ * stream layout) on buffers the caller owns, and allocates no device memory: it is for callers
+ * that own all device memory through their own allocator or arena, or that cannot afford the
+ * device synchronisation cudaMalloc/cudaFree may cause.  The outlet's previous-step jy column,
+ * the step's only other state, lives in a fixed 1 MiB __device__ array (2 x 65536 doubles) that
+ * every GPU loading the library holds until exit, so inner_h is limited to PLBM_NOALLOC_MAX_ROWS
+ * and larger domains are rejected with PLBM_ERR_ARGUMENT.
+ *   lattice0/1  device, 9 * P * inner_h doubles each, P = inner_w rounded up to a multiple of 32
+ *   flags       device, inner_w * inner_h int8, row-major from (x=1, y=1): 0 fluid, 1 solid
+ *   results     device, 4 * inner_w * inner_h doubles: rho | jx | jy | |j|, written on the last
+ *               step of the call
+ * first_step == 0 starts a run: it fills both lattices with the rest state, the results with
+ * rho = -1 / j = 0 and clears the jy column.  Step t reads lattice[t & 1] and writes
+ * lattice[(t + 1) & 1]; continue a run by passing first_step = the number of steps done.
+ * All calls share the jy array and it keeps the last call's contents: calls that overlap on the
+ * GPU (other streams or threads, or two runs interleaved) race on it.  The first call on each
+ * device fetches the array's device address (with that device current); make that first call
+ * before any stream capture.  Work is queued on `stream` (a cudaStream_t; NULL = legacy default
+ * stream) and not synchronised. */
+#define PLBM_NOALLOC_MAX_ROWS 65536
+typedef struct {
+    void *lattice0, *lattice1;
+    const int8_t *flags;
+    double *results;
+    unsigned inner_w, inner_h;
+    double relaxation_time;
+    double inlet_density, inlet_velocity_x, inlet_velocity_y;
+    double outlet_density, outlet_velocity_x, outlet_velocity_y;
+    unsigned first_step, steps;
+    int nan_protection;
+    void *stream;
+} plbm_noalloc_args;
+
+int plbm_nptl_steps_noalloc(const plbm_noalloc_args *args);
+/* Message of the last failed plbm_nptl_steps_noalloc call on this thread. */
+const char *plbm_noalloc_last_error(void);
+
 /* Last error message for h (or of the last failed create when h is NULL). */
 const char *plbm_last_error(const plbm_handler *h);
 const char *plbm_version(void);
