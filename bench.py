@@ -180,12 +180,12 @@ def dist_setup():
     return world, rank, local
 
 
-def max_over_ranks(v: float, world: int) -> float:
+def max_over_ranks(v: float, world: int, device: str = "cuda") -> float:
     if world == 1:
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

@@ -126,6 +126,16 @@ int plbm_properties_to_json(const plbm_properties *props, const char *path);
  * strings are copied into thread-local storage valid until the next call on this thread. */
 int plbm_json_to_properties(const char *path, int offset, plbm_properties *out);
 
+/* core::Domain(Properties&) (src/lbm/core/simulation.cpp:194-382) for these properties, without a
+ * GPU: out7 = {total_node_count, horizontal_nodes, vertical_nodes, subdomain_vertical_nodes,
+ * subdomain_horizontal_nodes, subdomain_count_vertical, subdomain_count_horizontal}.
+ * PLBM_ERR_PROPERTY when nsol's work-group size is below 6. */
+int plbm_compute_domain(const plbm_properties *props, unsigned out7[7]);
+/* The phase flags setup_domain (include/lbm/core/domain_initialization.hpp:453-518) gives the inner
+ * W*H nodes (row-major from (x=1, y=1); 0 fluid, 1 solid), without a GPU.  The porous scenario
+ * draws from the process-wide rand() sequence, as the reference does. */
+int plbm_make_flags(const plbm_properties *props, int8_t *out);
+
 /* ---- measurement hooks (no counterpart in the reference) ------------------------------ */
 
 /* Runs n steps synchronously on the calling thread with device-resident data; writes the

@@ -137,6 +137,9 @@ int plbmo_domain_for(int algorithm, unsigned wg, unsigned X, unsigned V, plbmo_d
         if (w & 0x1) w--;
         power_of_two_handling(w, &sv, &sh);
         sv -= 1; sh -= 2;
+        /* the power-of-4 branch can give 2x2 tiles (wg 20, 36, ...): the reference then divides by
+           zero in the subdomain count; report it instead */
+        if (sh == 0 || sv == 0) return -1;
     } else if (w & 0x1) {                    /* :268-273 / :301-306 */
         sh = (unsigned)w; sv = 1;
     } else {

@@ -26,7 +26,7 @@ import numpy as np
 __all__ = [
     "Properties", "create_handler", "AlgorithmHandler", "Exception", "PropertyArgumentException",
     "WaitException", "CudaException", "ParseException", "NoDeviceException", "PRECISIONS",
-    "properties_to_json", "json_to_properties", "library_path", "load_library",
+    "properties_to_json", "json_to_properties", "library_path", "load_library", "compute_domain", "make_flags",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -111,6 +111,8 @@ _SIGS = {
     "plbm_launches_per_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]),
     "plbm_bytes_per_node": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "plbm_mass_momentum": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "plbm_compute_domain": (ctypes.c_int, [ctypes.POINTER(_CProps), ctypes.POINTER(ctypes.c_uint)]),
+    "plbm_make_flags": (ctypes.c_int, [ctypes.POINTER(_CProps), ctypes.c_void_p]),
     "plbm_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "plbm_version": (ctypes.c_char_p, []),
 }
@@ -207,6 +209,26 @@ class Properties:
                 f"\tOutlet velocity: ({self.outlet_velocity_x:.6f}, {self.outlet_velocity_y:.6f})\n"
                 f"\tOutlet density: {self.outlet_density:.6f}\n"
                 f"\tRelaxation time: {self.relaxation_time:.6f}\n\n")
+
+
+_DOMAIN_KEYS = ("total_node_count", "horizontal_nodes", "vertical_nodes", "subdomain_vertical_nodes",
+                "subdomain_horizontal_nodes", "subdomain_count_vertical", "subdomain_count_horizontal")
+
+
+def compute_domain(props: Properties) -> dict:
+    """core::Domain(properties) (src/lbm/core/simulation.cpp:194-382), computed on the host."""
+    c = props._c()
+    arr = (ctypes.c_uint * 7)()
+    _check(load_library().plbm_compute_domain(ctypes.byref(c), arr))
+    return dict(zip(_DOMAIN_KEYS, list(arr)))
+
+
+def make_flags(props: Properties) -> np.ndarray:
+    """Inner (H, W) phase flags of the scenario (0 fluid, 1 solid), as setup_domain builds them."""
+    c = props._c()
+    out = np.empty((props.vertical_nodes - 2, props.horizontal_nodes - 2), dtype=np.int8)
+    _check(load_library().plbm_make_flags(ctypes.byref(c), out.ctypes.data))
+    return out
 
 
 def properties_to_json(props: Properties, path: str) -> None:

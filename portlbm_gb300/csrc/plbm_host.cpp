@@ -276,6 +276,11 @@ bool make_domain(const Props &p, Domain &d)
         power_of_two_handling(w, sv, sh);
         sv -= 1;
         sh -= 2;
+        // setup_for_swap with 2x2 tiles (which_power_of_4 returns 1, e.g. wg 20 or 100) leaves an
+        // empty subdomain and the reference divides by zero; refuse the size instead.
+        if (sh == 0 || sv == 0)
+            fail(PLBM_ERR_PROPERTY, "work-group size " + std::to_string(p.work_group_size) +
+                                        " gives the swap algorithm an empty subdomain (2x2 tiles minus its halo)");
     } else if (w & 0x1) {
         sh = (unsigned)w;
         sv = 1;
@@ -906,6 +911,28 @@ int plbm_json_to_properties(const char *path, int offset, plbm_properties *out)
         static thread_local Props keep;
         keep = json_to_props(path, offset, nullptr);
         *out = keep.to_c();
+    });
+}
+
+int plbm_compute_domain(const plbm_properties *props, unsigned out7[7])
+{
+    return guarded(nullptr, [&] {
+        const Props p = Props::make(*props);
+        Domain d{};
+        if (!make_domain(p, d)) fail(PLBM_ERR_PROPERTY, "work-group size below the swap algorithm's minimum of 6");
+        const unsigned v[7] = { d.total_node_count, d.horizontal_nodes, d.vertical_nodes, d.subdomain_vertical_nodes,
+                                d.subdomain_horizontal_nodes, d.subdomain_count_vertical, d.subdomain_count_horizontal };
+        std::memcpy(out7, v, sizeof v);
+    });
+}
+
+int plbm_make_flags(const plbm_properties *props, int8_t *out)
+{
+    return guarded(nullptr, [&] {
+        const Props p = Props::make(*props);
+        if (p.vertical_nodes < 4 || p.horizontal_nodes < 4) fail(PLBM_ERR_PROPERTY, "inner extents must be >= 2");
+        const std::vector<int8_t> f = make_flags(p, nullptr);
+        std::memcpy(out, f.data(), f.size());
     });
 }
 

@@ -74,3 +74,33 @@ def test_poiseuille_config_exact_10k_steps(plbm, oracle_mod):
     fast = run_gpu(plbm, "nptl", "stream", "Hagen-Poiseuille", 400, 100, 10000, wg=1024, rho_in=1.2,
                    precision="f64_fast")
     assert maxdiff(fast, ref) <= 1e-12
+
+
+GOLDEN_CASES = None
+
+
+def _golden():
+    import json
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    cases = json.load(open(os.path.join(here, "golden", "cases.json")))
+    return cases, np.load(os.path.join(here, "golden", "golden.npz"))
+
+
+_CASES, _ARRAYS = _golden()
+
+
+@pytest.mark.parametrize("case", _CASES, ids=[c["name"] for c in _CASES])
+def test_gpu_matches_reference_golden(plbm, case):
+    """GPU results equal the reference's own results (tests/golden, generated by running the
+    reference's algorithm classes) exactly: f64_strict for double cases, f32_ref for USE_FLOAT."""
+    import ctypes
+    if case["scenario"] == "porous":
+        ctypes.CDLL(None).srand(case["rand_seed"])
+    precision = "f64_strict" if case["precision"] == "f64" else "f32_ref"
+    got = run_gpu(plbm, case["algorithm"], case["data_layout"], case["scenario"], case["w"], case["h"],
+                  case["steps"], wg=case["work_group_size"], precision=precision, rho_in=case["inlet_density"],
+                  tau=case["relaxation_time"])
+    for k in ("rho", "jx", "jy", "jabs"):
+        ref = _ARRAYS[f"{case['name']}__{k}"]
+        assert np.array_equal(got[k], ref), f"{k}: max abs {np.max(np.abs(got[k] - ref))}"
