@@ -592,11 +592,12 @@ struct plbm_handler {
         // clamped to what the kernels can run; results do not depend on it.
         const unsigned sh = dom.subdomain_horizontal_nodes, sv = dom.subdomain_vertical_nodes;
         const int cap = plbm::max_threads_for(alg, prec, lay);
+        const unsigned ny = (alg == 0 || alg == 1) ? (unsigned)plbm::rows_per_thread(prec) : 1u;
         if (alg == 1) {
             unsigned t = std::min<unsigned>(std::max<unsigned>(props.work_group_size, 32u), (unsigned)cap);
             t = (t + 31) / 32 * 32;
             block = dim3(t);
-            grid = dim3((unsigned)((N + t - 1) / t));
+            grid = dim3((unsigned)((N + (unsigned long long)t * ny - 1) / ((unsigned long long)t * ny)));
         } else {
             unsigned bx = alg == 0 || alg == 3 ? std::max(32u, std::min(sh, 128u)) : std::min(sh, 64u);
             bx = std::max(1u, bx);
@@ -606,7 +607,7 @@ struct plbm_handler {
                 by = std::min(by, (unsigned)H);
             }
             block = dim3(bx, by);
-            grid = dim3((W + bx - 1) / bx, (H + by - 1) / by);
+            grid = dim3((W + bx - 1) / bx, (H + by * ny - 1) / (by * ny));
         }
         if (alg == 2) {
             b.tile_w = (int)block.x;

@@ -37,41 +37,75 @@ __device__ __forceinline__ CT<PREC> pull_one(const void *S, unsigned long long n
     return ld<PREC>(S, lidx<L>(s, d, p.N), d, p);
 }
 
-template <int PREC, int L>
-__device__ __forceinline__ void update_two_lattice(int xi, int yi, const StepParams &p)
+// Rows per thread: a node of the 2-byte forms moves only 36 B, so each thread issues the loads of
+// several nodes before computing any of them to keep enough bytes in flight per SM.
+template <int PREC> struct RowsPerThread { static constexpr int value = rows_per_thread(PREC); };
+
+template <int PREC, int L, int NY>
+__device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const int yi[NY], const StepParams &p)
 {
-    const unsigned long long n = (unsigned long long)xi + (unsigned long long)yi * p.P;
-    const uint16_t lk = p.links[n];
-    if (!(lk & LINK_FLUID)) return;
-    CT<PREC> f[9];
+    CT<PREC> f[NY][9];
+    uint16_t lk[NY];
+    unsigned long long n[NY];
 #pragma unroll
-    for (int d = 0; d < 9; ++d) f[d] = pull_one<PREC, L>(p.lat0, n, xi, yi, d, lk, p);
-    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
-    const Moments m = collide<PREC>(f, p);
+    for (int j = 0; j < NY; ++j) {
+        const bool in = xi[j] < p.W && yi[j] < p.H;
+        n[j] = in ? (unsigned long long)xi[j] + (unsigned long long)yi[j] * p.P : 0;
+        lk[j] = in ? p.links[n[j]] : 0;
+    }
 #pragma unroll
-    for (int d = 0; d < 9; ++d) st<PREC>(p.lat1, lidx<L>(n, d, p.N), d, f[d], p);
-    observables<PREC>(m, xi, yi, p);
+    for (int j = 0; j < NY; ++j)
+        if (lk[j] & LINK_FLUID) {
+#pragma unroll
+            for (int d = 0; d < 9; ++d) f[j][d] = pull_one<PREC, L>(p.lat0, n[j], xi[j], yi[j], d, lk[j], p);
+        }
+#pragma unroll
+    for (int j = 0; j < NY; ++j) {
+        if (!(lk[j] & LINK_FLUID)) continue;
+        if (is_outlet_row(xi[j], yi[j], p)) outlet_fill<PREC>(f[j], p.jy_prev[yi[j]], p);
+        const Moments m = collide<PREC>(f[j], p);
+#pragma unroll
+        for (int d = 0; d < 9; ++d) st<PREC>(p.lat1, lidx<L>(n[j], d, p.N), d, f[j][d], p);
+        observables<PREC>(m, xi[j], yi[j], p);
+    }
 }
 
-// nptl: 2-D blocks (tile shape from the work-group size hint).
+// nptl: 2-D blocks (tile shape from the work-group size hint); each thread updates NY
+// consecutive rows of its column.
 template <int PREC, int L>
 __global__ void k_nptl(StepParams p)
 {
-    const int xi = blockIdx.x * blockDim.x + threadIdx.x;
-    const int yi = blockIdx.y * blockDim.y + threadIdx.y;
-    if (xi >= p.W || yi >= p.H) return;
-    update_two_lattice<PREC, L>(xi, yi, p);
+    constexpr int NY = RowsPerThread<PREC>::value;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y0 = (blockIdx.y * blockDim.y + threadIdx.y) * NY;
+    if (x >= p.W || y0 >= p.H) return;
+    int xi[NY], yi[NY];
+#pragma unroll
+    for (int j = 0; j < NY; ++j) { xi[j] = x; yi[j] = y0 + j; }
+    update_two_lattice_rows<PREC, L, NY>(xi, yi, p);
 }
 
-// lptl: 1-D launch over n = x' + y' * P (padding columns x' >= W idle).
+// lptl: 1-D launch over n = x' + y' * P (padding columns x' >= W idle); each thread updates NY
+// nodes one grid-width apart.
 template <int PREC, int L>
 __global__ void k_lptl(StepParams p)
 {
-    const unsigned long long n = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= p.N) return;
-    const int yi = (int)(n / (unsigned)p.P), xi = (int)(n - (unsigned long long)yi * p.P);
-    if (xi >= p.W) return;
-    update_two_lattice<PREC, L>(xi, yi, p);
+    constexpr int NY = RowsPerThread<PREC>::value;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long n0 = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int xi[NY], yi[NY];
+#pragma unroll
+    for (int j = 0; j < NY; ++j) {
+        const unsigned long long n = n0 + j * stride;
+        if (n < p.N) {
+            yi[j] = (int)(n / (unsigned)p.P);
+            xi[j] = (int)(n - (unsigned long long)yi[j] * p.P);
+        } else {
+            yi[j] = p.H;
+            xi[j] = p.W;
+        }
+    }
+    update_two_lattice_rows<PREC, L, NY>(xi, yi, p);
 }
 
 // ---- npol: in place, one tile per thread block --------------------------------------------

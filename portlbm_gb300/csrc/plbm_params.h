@@ -10,6 +10,9 @@ enum Precision { F64_STRICT = 0, F64_FAST = 1, F32_REF = 2, F32 = 3, F16S = 4, B
 
 constexpr uint16_t LINK_FLUID = 1u << 4;
 
+// Nodes per thread of the two-lattice kernels (nptl rows, lptl grid strides), per precision.
+constexpr int rows_per_thread(int prec) { return prec == F32 ? 2 : (prec == F16S || prec == BF16S) ? 4 : 1; }
+
 // Step parameters, passed by value to every step kernel.
 struct StepParams {
     void *lat0;                 // source lattice (two-lattice) / the lattice (one-lattice)
