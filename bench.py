@@ -37,7 +37,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 W_DEFAULT, H_DEFAULT = 8192, 8192
-BYTES_PER_NODE = {"f64_strict": 144.0, "f64_fast": 144.0, "f32_ref": 72.0, "f32": 72.0, "f16s": 36.0, "bf16s": 36.0}
+BYTES_PER_NODE = {"f64_strict": 144.0, "f64_fast": 144.0, "f64_q60": 144.0, "f32_ref": 72.0, "f32": 72.0,
+                  "f16s": 36.0, "bf16s": 36.0}
 
 
 def circle_channel_mask(w: int, h: int) -> np.ndarray:

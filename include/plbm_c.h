@@ -49,8 +49,12 @@ enum { PLBM_DENSITY = 0, PLBM_X_VELOCITY = 1, PLBM_Y_VELOCITY = 2, PLBM_ABS_VELO
  * update into fewer FP64 instructions (FMA) and agrees to <= 1e-12.  F32_REF restates the
  * reference's USE_FLOAT build (include/lbm/core/constants.hpp:17-21).  F32, F16S and BF16S
  * store populations in float / half / bfloat16 (the latter two shifted by w_i * rho0) and
- * collide in FP32. */
-enum { PLBM_F64_STRICT = 0, PLBM_F64_FAST = 1, PLBM_F32_REF = 2, PLBM_F32 = 3, PLBM_F16S = 4, PLBM_BF16S = 5 };
+ * collide in FP32.  F64_Q60 keeps FP64 accuracy (populations as 64-bit fixed point,
+ * round(f * 2^60), finer than an FP64 ulp for |f| >= 2^-7) and collides on the integer pipe,
+ * which GB300 issues ~38x faster than FP64; agrees with F64_STRICT to <= 1e-12 and fails with
+ * PLBM_ERR_NUMERIC if a population leaves [-4, 4). */
+enum { PLBM_F64_STRICT = 0, PLBM_F64_FAST = 1, PLBM_F32_REF = 2, PLBM_F32 = 3, PLBM_F16S = 4, PLBM_BF16S = 5,
+       PLBM_F64_Q60 = 6 };
 
 typedef struct plbm_handler plbm_handler;
 

@@ -49,6 +49,7 @@ template <> struct Store<F32_REF> { using T = float; using C = float; };
 template <> struct Store<F32> { using T = float; using C = float; };
 template <> struct Store<F16S> { using T = __half; using C = float; };
 template <> struct Store<BF16S> { using T = __nv_bfloat16; using C = float; };
+template <> struct Store<F64_Q60> { using T = long long; using C = long long; };
 
 // Loads / stores between storage and compute type.  The FP16/BF16 forms store f - w_d * rho0
 // (rho0 = 1), which keeps the stored magnitudes small and the rounding error relative to the
@@ -231,12 +232,97 @@ __device__ __forceinline__ Moments collide_f32(float f[9], float omega)
     return { (double)rho, (double)jx, (double)jy, (double)usq };
 }
 
+// ---- F64_Q60: FP64-accuracy populations in 64-bit fixed point ------------------------------
+// GB300 issues FP64 at 0.5 T instructions/s but 64-bit integer multiply-adds (as 32-bit IMADs) at
+// ~19 T/s.  The Q60 form stores each population as round(f * 2^60) in an int64 (Q3.60: |f| < 8,
+// resolution 2^-60 ~ 8.7e-19, finer than an FP64 ulp of any population >= 2^-7) and performs the
+// BGK update exactly like F64_FAST but on the integer pipe.  Products take the 128-bit product's
+// bits 60..123.  A population leaving [-4, 4) sets *status; the host then reports an error.
+
+__device__ __forceinline__ long long mulq(long long a, long long b)
+{
+    const long long hi = __mul64hi(a, b);
+    const unsigned long long lo = (unsigned long long)a * (unsigned long long)b;
+    return (long long)(((unsigned long long)hi << 4) | (lo >> 60));
+}
+
+// Nearest double (ties to even) of v * 2^-60.
+__device__ __forceinline__ double q_to_double(long long v)
+{
+    if (v == 0) return 0.0;
+    const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
+    const unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+    const int lz = __clzll((long long)a);
+    const unsigned long long n = a << lz;
+    unsigned long long mant = n >> 11;
+    const unsigned long long rem = n & 0x7FFull;
+    mant += (rem > 0x400ull) | ((rem == 0x400ull) & (mant & 1ull));
+    // exponent field = 1026 - lz; mant carries the implicit bit (and a rounding carry) into it
+    return __longlong_as_double((long long)(sgn | ((((unsigned long long)(1025 - lz)) << 52) + mant)));
+}
+
+// v * 2^60 truncated toward zero; |d| < 8.
+__device__ __forceinline__ long long double_to_q(double d)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0) return 0;
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = e - 1015;
+    const long long v = sh >= 0 ? (long long)(m << sh) : (sh <= -64 ? 0 : (long long)(m >> -sh));
+    return (b >> 63) ? -v : v;
+}
+
+__device__ __forceinline__ unsigned long long q_out_of_range(long long v)
+{
+    return ((unsigned long long)(v + (1ll << 62))) >> 63;   // 1 unless -4 <= v * 2^-60 < 4
+}
+
+__device__ __forceinline__ Moments collide_q60(long long f[9], const StepParams &p)
+{
+    const long long A = f[2] + f[5] + f[8], B = f[0] + f[3] + f[6];
+    const long long C = f[6] + f[7] + f[8], E = f[0] + f[1] + f[2];
+    const long long rho = (B + (f[1] + f[4] + f[7])) + A;
+    const long long jx = A - B, jy = C - E;
+    const long long usq = mulq(jx, jx) + mulq(jy, jy);
+    const long long R = rho - (usq + (usq >> 1));
+    const long long b9 = mulq(p.q_ow9, R), b36 = mulq(p.q_ow36, R);
+    f[4] = mulq(p.q_om1, f[4]) + mulq(p.q_ow49, R);
+    {
+        const long long u = jx, sym = mulq(mulq(p.q_k9, u), u) + b9, ou = mulq(p.q_o9, u);
+        f[5] = mulq(p.q_om1, f[5]) + sym + ou;
+        f[3] = mulq(p.q_om1, f[3]) + sym - ou;
+    }
+    {
+        const long long u = jy, sym = mulq(mulq(p.q_k9, u), u) + b9, ou = mulq(p.q_o9, u);
+        f[7] = mulq(p.q_om1, f[7]) + sym + ou;
+        f[1] = mulq(p.q_om1, f[1]) + sym - ou;
+    }
+    {
+        const long long u = jx + jy, sym = mulq(mulq(p.q_k36, u), u) + b36, ou = mulq(p.q_o36, u);
+        f[8] = mulq(p.q_om1, f[8]) + sym + ou;
+        f[0] = mulq(p.q_om1, f[0]) + sym - ou;
+    }
+    {
+        const long long u = jx - jy, sym = mulq(mulq(p.q_k36, u), u) + b36, ou = mulq(p.q_o36, u);
+        f[2] = mulq(p.q_om1, f[2]) + sym + ou;
+        f[6] = mulq(p.q_om1, f[6]) + sym - ou;
+    }
+    unsigned long long bad = 0;
+#pragma unroll
+    for (int d = 0; d < 9; ++d) bad |= q_out_of_range(f[d]);
+    if (bad) atomicOr(p.status, 1);
+    // the moments travel as raw fixed-point bits; observables<F64_Q60> converts them when needed
+    return { __longlong_as_double(rho), __longlong_as_double(jx), __longlong_as_double(jy), __longlong_as_double(usq) };
+}
+
 template <int PREC>
 __device__ __forceinline__ Moments collide(typename Store<PREC>::C f[9], const StepParams &p)
 {
     if constexpr (PREC == F64_STRICT) return collide_f64_strict(f, p.omega);
     else if constexpr (PREC == F64_FAST) return collide_f64_fast(f, p.omega);
     else if constexpr (PREC == F32_REF) return collide_f32_ref(f, p.omegaf);
+    else if constexpr (PREC == F64_Q60) return collide_q60(f, p);
     else return collide_f32(f, p.omegaf);
 }
 
@@ -256,6 +342,13 @@ __device__ __forceinline__ void outlet_fill(typename Store<PREC>::C f[9], double
         f[0] = __dsub_rn(__dsub_rn(__dsub_rn(g0, hd), x6), hy);
         f[3] = __dsub_rn(g1, __dmul_rn(2.0 / 3, xv));
         f[6] = __dadd_rn(__dsub_rn(__dadd_rn(g2, hd), x6), hy);
+    } else if constexpr (PREC == F64_Q60) {
+        const long long xv = -p.q_rho_out + ((f[1] + f[4] + f[7]) + 2 * (f[8] + f[5] + f[2]));
+        const long long hd = (f[1] - f[7]) >> 1, x6 = mulq(p.q_sixth, xv), hy = double_to_q(jyo) >> 1;
+        const long long g0 = f[8], g1 = f[5], g2 = f[2];
+        f[0] = g0 - hd - x6 - hy;
+        f[3] = g1 - mulq(p.q_two_thirds, xv);
+        f[6] = g2 + hd - x6 + hy;
     } else if constexpr (PREC == F32_REF) {
         const float xv = __fadd_rn(-p.rho_outf,
                                    __fadd_rn(__fadd_rn(__fadd_rn(f[1], f[4]), f[7]),
@@ -281,15 +374,18 @@ __device__ __forceinline__ void outlet_fill(typename Store<PREC>::C f[9], double
 // (x = 0), feq(outlet) (x = X-1).
 template <int PREC> __device__ __forceinline__ typename Store<PREC>::C g_weight(const StepParams &p, int d)
 {
-    if constexpr (sizeof(typename Store<PREC>::C) == 8) return p.weight[d]; else return p.weightf[d];
+    if constexpr (PREC == F64_Q60) return p.q_weight[d];
+    else if constexpr (sizeof(typename Store<PREC>::C) == 8) return p.weight[d]; else return p.weightf[d];
 }
 template <int PREC> __device__ __forceinline__ typename Store<PREC>::C g_in(const StepParams &p, int d)
 {
-    if constexpr (sizeof(typename Store<PREC>::C) == 8) return p.feq_in[d]; else return p.feq_inf[d];
+    if constexpr (PREC == F64_Q60) return p.q_feq_in[d];
+    else if constexpr (sizeof(typename Store<PREC>::C) == 8) return p.feq_in[d]; else return p.feq_inf[d];
 }
 template <int PREC> __device__ __forceinline__ typename Store<PREC>::C g_out(const StepParams &p, int d)
 {
-    if constexpr (sizeof(typename Store<PREC>::C) == 8) return p.feq_out[d]; else return p.feq_outf[d];
+    if constexpr (PREC == F64_Q60) return p.q_feq_out[d];
+    else if constexpr (sizeof(typename Store<PREC>::C) == 8) return p.feq_out[d]; else return p.feq_outf[d];
 }
 
 // Writes the macroscopic observables of node (x', y') when this step is copied to the host,
@@ -322,8 +418,16 @@ __device__ __forceinline__ void write_observables_f32ref(const Moments &m, int x
 template <int PREC>
 __device__ __forceinline__ void observables(const Moments &m, int xi, int yi, const StepParams &p)
 {
-    if constexpr (PREC == F32_REF) write_observables_f32ref(m, xi, yi, p);
-    else write_observables(m, xi, yi, p);
+    if constexpr (PREC == F32_REF) {
+        write_observables_f32ref(m, xi, yi, p);
+    } else if constexpr (PREC == F64_Q60) {
+        if (!p.write_results && xi != p.W - 2) return;
+        const Moments d = { q_to_double(__double_as_longlong(m.rho)), q_to_double(__double_as_longlong(m.jx)),
+                            q_to_double(__double_as_longlong(m.jy)), q_to_double(__double_as_longlong(m.usq)) };
+        write_observables(d, xi, yi, p);
+    } else {
+        write_observables(m, xi, yi, p);
+    }
 }
 
 // True when node (x', y') is an outlet border node whose 0/3/6 populations come from the

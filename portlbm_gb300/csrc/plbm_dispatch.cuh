@@ -9,4 +9,5 @@
     PLBM_CASE(KER, 2, 0) PLBM_CASE(KER, 2, 1) PLBM_CASE(KER, 2, 2)                             \
     PLBM_CASE(KER, 3, 0) PLBM_CASE(KER, 3, 1) PLBM_CASE(KER, 3, 2)                             \
     PLBM_CASE(KER, 4, 0) PLBM_CASE(KER, 4, 1) PLBM_CASE(KER, 4, 2)                             \
-    PLBM_CASE(KER, 5, 0) PLBM_CASE(KER, 5, 1) PLBM_CASE(KER, 5, 2)
+    PLBM_CASE(KER, 5, 0) PLBM_CASE(KER, 5, 1) PLBM_CASE(KER, 5, 2)                             \
+    PLBM_CASE(KER, 6, 0) PLBM_CASE(KER, 6, 1) PLBM_CASE(KER, 6, 2)

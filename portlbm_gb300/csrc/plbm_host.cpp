@@ -139,10 +139,11 @@ struct JsonExtras {
 
 int precision_from_name(const std::string &s)
 {
-    static const char *names[] = { "f64_strict", "f64_fast", "f32_ref", "f32", "f16s", "bf16s" };
-    for (int i = 0; i < 6; ++i)
+    static const char *names[] = { "f64_strict", "f64_fast", "f32_ref", "f32", "f16s", "bf16s", "f64_q60" };
+    for (int i = 0; i < 7; ++i)
         if (s == names[i]) return i;
-    fail(PLBM_ERR_PROPERTY, "Unknown gb300.precision: \"" + s + "\". Valid values: f64_strict, f64_fast, f32_ref, f32, f16s, bf16s");
+    fail(PLBM_ERR_PROPERTY,
+         "Unknown gb300.precision: \"" + s + "\". Valid values: f64_strict, f64_fast, f32_ref, f32, f16s, bf16s, f64_q60");
 }
 
 // json_to_properties(path, offset): the node counts read are inner extents plus `offset`, and the
@@ -380,7 +381,10 @@ void maxwell_boltzmann(R ux, R uy, R rho, R *t)
 
 int alg_index(const std::string &a) { return a == "nptl" ? 0 : a == "lptl" ? 1 : a == "npol" ? 2 : 3; }
 int layout_index(const std::string &l) { return l == "collision" ? 0 : l == "stream" ? 1 : 2; }
-size_t storage_bytes(int prec) { return prec <= 1 ? 8 : prec <= 3 ? 4 : 2; }
+size_t storage_bytes(int prec) { return (prec <= 1 || prec == PLBM_F64_Q60) ? 8 : prec <= 3 ? 4 : 2; }
+
+// round(x * 2^60) for the Q60 form's constants, evaluated in long double.
+long long q60(long double x) { return (long long)std::llroundl(x * 1152921504606846976.0L); }
 
 thread_local std::string g_tls_error;
 std::mutex g_create_mu;
@@ -412,6 +416,7 @@ struct plbm_handler {
     double *jy_d = nullptr;
     void *halo[2] = { nullptr, nullptr };
     double *red_d = nullptr;
+    int *status_d = nullptr;
     double *res_h[4] = { nullptr, nullptr, nullptr, nullptr };
     size_t nres = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -448,7 +453,8 @@ struct plbm_handler {
         if (flags_d) cudaFree(flags_d);
         if (jy_d) cudaFree(jy_d);
         if (red_d) cudaFree(red_d);
-        links = nullptr; flags_d = nullptr; jy_d = nullptr; red_d = nullptr;
+        if (status_d) cudaFree(status_d);
+        links = nullptr; flags_d = nullptr; jy_d = nullptr; red_d = nullptr; status_d = nullptr;
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         ev0 = ev1 = nullptr;
@@ -477,7 +483,7 @@ struct plbm_handler {
         prec = opt.precision;
         if (ex.precision >= 0 && !opt_precision_set) prec = ex.precision;
         if (ex.nan_protection >= 0) opt.nan_protection = ex.nan_protection;
-        if (prec < 0 || prec > 5) fail(PLBM_ERR_ARGUMENT, "precision must be one of PLBM_F64_STRICT..PLBM_BF16S");
+        if (prec < 0 || prec > 6) fail(PLBM_ERR_ARGUMENT, "precision must be one of PLBM_F64_STRICT..PLBM_F64_Q60");
 
         int ndev = 0;
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) fail(PLBM_ERR_NO_DEVICE, "no CUDA device available");
@@ -550,6 +556,8 @@ struct plbm_handler {
         cuda_check(cudaMalloc(&jy_d, 2ull * H * sizeof(double)), "cudaMalloc jy");
         cuda_check(cudaMemsetAsync(jy_d, 0, 2ull * H * sizeof(double), stream), "memset jy");
         cuda_check(cudaMalloc(&red_d, 3 * sizeof(double)), "cudaMalloc reduce");
+        cuda_check(cudaMalloc(&status_d, sizeof(int)), "cudaMalloc status");
+        cuda_check(cudaMemsetAsync(status_d, 0, sizeof(int), stream), "memset status");
         cuda_check(cudaMemcpyAsync(flags_d, flags.data(), nres, cudaMemcpyHostToDevice, stream), "H2D flags");
         cuda_check(plbm::launch_links(flags_d, links, W, H, P, stream), "links kernel");
         cuda_check(plbm::launch_fill_results(res_d[0], res_d[1], res_d[2], res_d[3], nres, stream), "results fill");
@@ -557,7 +565,7 @@ struct plbm_handler {
         // Ghost constants and rest state in the arithmetic of the chosen form.
         plbm::StepParams &b = base;
         std::memset(&b, 0, sizeof b);
-        if (prec == PLBM_F64_STRICT || prec == PLBM_F64_FAST) {
+        if (prec == PLBM_F64_STRICT || prec == PLBM_F64_FAST || prec == PLBM_F64_Q60) {
             maxwell_boltzmann<double>(0, 0, 1, b.weight);
             maxwell_boltzmann<double>(props.ivx, props.ivy, props.irho, b.feq_in);
             maxwell_boltzmann<double>(props.ovx, props.ovy, props.orho, b.feq_out);
@@ -579,6 +587,28 @@ struct plbm_handler {
         }
         b.omegaf = (float)b.omega;
         b.rho_outf = (float)b.rho_out;
+        {
+            // Q60 constants from the reference's double constants (1/tau, w_d, 1.0/6, 2.0/3)
+            const long double om = (long double)b.omega, w9 = 1.0 / 9, w36 = 1.0 / 36, w49 = 4.0 / 9;
+            b.q_om1 = q60(1.0L - om);
+            b.q_ow49 = q60(om * w49); b.q_ow9 = q60(om * w9); b.q_ow36 = q60(om * w36);
+            b.q_k9 = q60(4.5L * om * w9); b.q_k36 = q60(4.5L * om * w36);
+            b.q_o9 = q60(3.0L * om * w9); b.q_o36 = q60(3.0L * om * w36);
+            b.q_rho_out = q60((long double)b.rho_out);
+            b.q_sixth = q60((long double)(1.0 / 6));
+            b.q_two_thirds = q60((long double)(2.0 / 3));
+            for (int d = 0; d < 9; ++d) {
+                b.q_weight[d] = q60((long double)b.weight[d]);
+                b.q_feq_in[d] = q60((long double)b.feq_in[d]);
+                b.q_feq_out[d] = q60((long double)b.feq_out[d]);
+            }
+            b.status = status_d;
+            if (prec == PLBM_F64_Q60) {
+                for (int d = 0; d < 9; ++d)
+                    if (std::fabs(b.feq_in[d]) >= 4 || std::fabs(b.feq_out[d]) >= 4)
+                        fail(PLBM_ERR_NUMERIC, "f64_q60 needs boundary populations in [-4, 4); use f64_strict");
+            }
+        }
         for (int i = 0; i < (two_lattice() ? 2 : 1); ++i)
             cuda_check(plbm::launch_fill_lattice(lat[i], prec, lay, N, b.weight, stream), "lattice fill");
 
@@ -674,6 +704,17 @@ struct plbm_handler {
         for (; t < t1; ++t) cuda_check(launch_step(t, false), "step");
     }
 
+    // The Q60 form records a population that left its fixed-point range in a device word.
+    void check_status()
+    {
+        if (prec != PLBM_F64_Q60) return;
+        int st = 0;
+        cuda_check(cudaMemcpyAsync(&st, status_d, sizeof(int), cudaMemcpyDeviceToHost, stream), "status");
+        cuda_check(cudaStreamSynchronize(stream), "status");
+        if (st)
+            fail(PLBM_ERR_NUMERIC, "a population left the f64_q60 range [-4, 4) (unstable run?); rerun with f64_strict");
+    }
+
     void copy_results()
     {
         for (int i = 0; i < 4; ++i)
@@ -700,9 +741,11 @@ struct plbm_handler {
                     end = std::min(frame, t + chunk);
                     run_plain(t, end);
                     cuda_check(cudaStreamSynchronize(stream), "step");
+                    check_status();
                 } else {
                     cuda_check(launch_step(t, true), "step");
                     copy_results();
+                    check_status();
                     end = t + 1;
                 }
                 const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c0).count();
@@ -748,7 +791,7 @@ int guarded(plbm_handler *h, F &&f)
 int plbm::max_threads_for(int alg, int prec, int lay)
 {
     (void)alg; (void)lay;
-    return prec == PLBM_F64_STRICT || prec == PLBM_F32_REF ? 256 : 512;
+    return prec == PLBM_F64_STRICT || prec == PLBM_F32_REF || prec == PLBM_F64_Q60 ? 256 : 512;
 }
 
 extern "C" {
@@ -953,6 +996,7 @@ int plbm_run_steps(plbm_handler *h, unsigned n, double *ms_per_step)
         float ms = 0;
         cuda_check(cudaEventElapsedTime(&ms, h->ev0, h->ev1), "elapsed");
         if (ms_per_step) *ms_per_step = ms / n;
+        h->check_status();
         h->iteration = t0 + n;
         h->progress = (double)(t0 + n) / (double)h->props.time_steps;
     });

@@ -6,12 +6,12 @@
 namespace plbm {
 
 enum Layout { COLLISION = 0, STREAM = 1, BUNDLE = 2 };
-enum Precision { F64_STRICT = 0, F64_FAST = 1, F32_REF = 2, F32 = 3, F16S = 4, BF16S = 5 };
+enum Precision { F64_STRICT = 0, F64_FAST = 1, F32_REF = 2, F32 = 3, F16S = 4, BF16S = 5, F64_Q60 = 6 };
 
 constexpr uint16_t LINK_FLUID = 1u << 4;
 
 // Nodes per thread of the two-lattice kernels (nptl rows, lptl grid strides), per precision.
-constexpr int rows_per_thread(int prec) { return prec == F32 ? 2 : (prec == F16S || prec == BF16S) ? 4 : 1; }
+constexpr int rows_per_thread(int) { return 1; }
 
 // Step parameters, passed by value to every step kernel.
 struct StepParams {
@@ -33,6 +33,11 @@ struct StepParams {
     // would run on the FP64 pipe)
     float feq_inf[9], feq_outf[9], weightf[9];
     float omegaf, rho_outf;
+    // F64_Q60: 64-bit fixed-point constants (value * 2^60, rounded from the double constants) and
+    // the device word that records a population leaving the fixed-point range
+    long long q_weight[9], q_feq_in[9], q_feq_out[9];
+    long long q_om1, q_ow49, q_ow9, q_ow36, q_k9, q_k36, q_o9, q_o36, q_rho_out, q_sixth, q_two_thirds;
+    int *status;
     int outlet_mode;            // 0: Zou/He-type density outlet; 1: constant feq(outlet) ghost
     int nan_protection;
     int write_results;          // this step is copied to the host

@@ -45,7 +45,8 @@ __global__ void k_fill_lattice(void *lat, int lay, unsigned long long N, W9 w)
         else if (lay == STREAM) d = (int)(i / N);
         else d = 3 * (int)(i / (3 * N)) + (int)((i % (3 * N)) % 3);
         T *b = static_cast<T *>(lat);
-        if constexpr (PREC == F16S) b[i] = __float2half_rn(0.0f);
+        if constexpr (PREC == F64_Q60) b[i] = double_to_q(w.w[d]);
+        else if constexpr (PREC == F16S) b[i] = __float2half_rn(0.0f);
         else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(0.0f);
         else b[i] = (T)w.w[d];
     }
@@ -61,6 +62,7 @@ cudaError_t launch_fill_lattice(void *lat, int prec, int lay, unsigned long long
     case F32_REF: case F32: k_fill_lattice<F32><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
     case F16S: k_fill_lattice<F16S><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
     case BF16S: k_fill_lattice<BF16S><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
+    case F64_Q60: k_fill_lattice<F64_Q60><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -79,7 +81,8 @@ __global__ void k_fill_halo(void *halo, unsigned long long ncol, unsigned long l
         if (i < ncol) d = k < 3 ? 3 * k + 2 : 3 * (k - 3);
         else d = k < 3 ? 6 + k : k - 3;
         T *b = static_cast<T *>(halo);
-        if constexpr (PREC == F16S) b[i] = __float2half_rn(0.0f);
+        if constexpr (PREC == F64_Q60) b[i] = double_to_q(w.w[d]);
+        else if constexpr (PREC == F16S) b[i] = __float2half_rn(0.0f);
         else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(0.0f);
         else b[i] = (T)w.w[d];
     }
@@ -97,6 +100,7 @@ cudaError_t launch_fill_halo(void *halo, int prec, int W, int H, int ncb, int nr
     case F32_REF: case F32: k_fill_halo<F32><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
     case F16S: k_fill_halo<F16S><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
     case BF16S: k_fill_halo<BF16S><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
+    case F64_Q60: k_fill_halo<F64_Q60><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

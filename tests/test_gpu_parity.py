@@ -52,6 +52,21 @@ def test_fast_within_tolerance(plbm, oracle_mod, alg):
     assert maxdiff(got, ref) <= 1e-12
 
 
+@pytest.mark.parametrize("alg", ALGS)
+@pytest.mark.parametrize("lay", LAYOUTS)
+def test_q60_within_tolerance(plbm, oracle_mod, alg, lay):
+    """The integer-pipe FP64-accuracy form agrees with the reference arithmetic to <= 1e-12."""
+    ref = run_oracle(oracle_mod, alg, lay, "circle", 62, 30, 300)
+    got = run_gpu(plbm, alg, lay, "circle", 62, 30, 300, precision="f64_q60")
+    assert maxdiff(got, ref) <= 1e-12
+
+
+def test_q60_rejects_out_of_range_boundary(plbm):
+    props = plbm.Properties("nptl", "stream", False, 64, 10, 10, "circle", 30, 62, 0.0, 0.0, 10.0, 0.0, 0.0, 1.0, 0.6)
+    with pytest.raises(plbm.Exception, match="f64_q60"):
+        plbm.create_handler(props, precision="f64_q60")
+
+
 @pytest.mark.parametrize("alg,w,wg", [("npol", 65, 64), ("nsol", 61, 64), ("npol", 33, 16), ("nsol", 33, 16)])
 def test_buffered_outlet_case(plbm, oracle_mod, alg, w, wg):
     ref = run_oracle(oracle_mod, alg, "stream", "Hagen-Poiseuille", w, 20, 300, wg=wg)
@@ -71,9 +86,10 @@ def test_poiseuille_config_exact_10k_steps(plbm, oracle_mod):
     ref = run_oracle(oracle_mod, "nptl", "stream", "Hagen-Poiseuille", 400, 100, 10000, wg=1024, rho_in=1.2)
     got = run_gpu(plbm, "nptl", "stream", "Hagen-Poiseuille", 400, 100, 10000, wg=1024, rho_in=1.2)
     assert maxdiff(got, ref) == 0.0
-    fast = run_gpu(plbm, "nptl", "stream", "Hagen-Poiseuille", 400, 100, 10000, wg=1024, rho_in=1.2,
-                   precision="f64_fast")
-    assert maxdiff(fast, ref) <= 1e-12
+    for prec in ("f64_fast", "f64_q60"):
+        got = run_gpu(plbm, "nptl", "stream", "Hagen-Poiseuille", 400, 100, 10000, wg=1024, rho_in=1.2,
+                      precision=prec)
+        assert maxdiff(got, ref) <= 1e-12, prec
 
 
 GOLDEN_CASES = None
