@@ -233,17 +233,36 @@ __device__ __forceinline__ Moments collide_f32(float f[9], float omega)
 }
 
 // ---- F64_Q60: FP64-accuracy populations in 64-bit fixed point ------------------------------
-// GB300 issues FP64 at 0.5 T instructions/s but 64-bit integer multiply-adds (as 32-bit IMADs) at
-// ~19 T/s.  The Q60 form stores each population as round(f * 2^60) in an int64 (Q3.60: |f| < 8,
-// resolution 2^-60 ~ 8.7e-19, finer than an FP64 ulp of any population >= 2^-7) and performs the
-// BGK update exactly like F64_FAST but on the integer pipe.  Products take the 128-bit product's
-// bits 60..123.  A population leaving [-4, 4) sets *status; the host then reports an error.
+// GB300 issues FP64 at 0.5 T instructions/s but 32-bit integer multiply-adds at ~19 T/s.  The Q60
+// form stores each population as round(f * 2^60) in an int64 (Q3.60, resolution 2^-60 ~ 8.7e-19,
+// finer than an FP64 ulp of any population >= 2^-7) and performs the BGK update of F64_FAST on the
+// integer pipe.  Constants below 1 are held in Q0.64 so a product is the high word of a 64x64
+// multiply (within 2 units of 2^-60).  A population leaving [-4, 4) or a momentum leaving [-2, 2)
+// sets *status; the host then reports an error.
 
-__device__ __forceinline__ long long mulq(long long a, long long b)
+// High 64 bits of the 128-bit product of unsigned a and b from three 32x32 partial products; the
+// dropped low partial product and carries make it at most 2 units low.
+__device__ __forceinline__ unsigned long long umulhi_approx(unsigned long long a, unsigned long long b)
 {
-    const long long hi = __mul64hi(a, b);
-    const unsigned long long lo = (unsigned long long)a * (unsigned long long)b;
-    return (long long)(((unsigned long long)hi << 4) | (lo >> 60));
+    const unsigned al = (unsigned)a, ah = (unsigned)(a >> 32), bl = (unsigned)b, bh = (unsigned)(b >> 32);
+    return (unsigned long long)ah * bh + __umulhi(ah, bl) + __umulhi(al, bh);
+}
+
+// c * v for a constant c in [0, 1) held as round(c * 2^64) and a Q60 value v; result Q60.
+__device__ __forceinline__ long long mulc(unsigned long long c, long long v)
+{
+    const unsigned long long r = umulhi_approx(c, (unsigned long long)v);
+    return (long long)(v < 0 ? r - c : r);
+}
+
+// a * b for Q60 values with |a|, |b| < 2 (checked by the caller); result Q60.
+__device__ __forceinline__ long long mulv(long long a, long long b)
+{
+    const long long a2 = a << 2, b2 = b << 2;   // Q62
+    unsigned long long r = umulhi_approx((unsigned long long)a2, (unsigned long long)b2);
+    if (a2 < 0) r -= (unsigned long long)b2;
+    if (b2 < 0) r -= (unsigned long long)a2;
+    return (long long)r;
 }
 
 // Nearest double (ties to even) of v * 2^-60.
@@ -278,37 +297,45 @@ __device__ __forceinline__ unsigned long long q_out_of_range(long long v)
     return ((unsigned long long)(v + (1ll << 62))) >> 63;   // 1 unless -4 <= v * 2^-60 < 4
 }
 
+// The BGK update of F64_FAST in Q60: f' = f - omega f + omega feq with
+// omega feq_d = omega w_d (rho - 1.5 u^2) + 4.5 omega w_d cu^2 + 3 omega w_d cu.  Every constant is
+// below 1 for relaxation_time > 0.5 and is applied with mulc; omega f uses omega/2 twice.
 __device__ __forceinline__ Moments collide_q60(long long f[9], const StepParams &p)
 {
     const long long A = f[2] + f[5] + f[8], B = f[0] + f[3] + f[6];
     const long long C = f[6] + f[7] + f[8], E = f[0] + f[1] + f[2];
     const long long rho = (B + (f[1] + f[4] + f[7])) + A;
     const long long jx = A - B, jy = C - E;
-    const long long usq = mulq(jx, jx) + mulq(jy, jy);
+    const long long jx2 = mulv(jx, jx), jy2 = mulv(jy, jy), jxy = mulv(jx, jy);
+    const long long usq = jx2 + jy2;
     const long long R = rho - (usq + (usq >> 1));
-    const long long b9 = mulq(p.q_ow9, R), b36 = mulq(p.q_ow36, R);
-    f[4] = mulq(p.q_om1, f[4]) + mulq(p.q_ow49, R);
+    const unsigned long long wh = (unsigned long long)p.q_om1;   // omega / 2, Q64
+    const long long b9 = mulc((unsigned long long)p.q_ow9, R), b36 = mulc((unsigned long long)p.q_ow36, R);
+    f[4] = f[4] + mulc((unsigned long long)p.q_ow49, R) - 2 * mulc(wh, f[4]);
     {
-        const long long u = jx, sym = mulq(mulq(p.q_k9, u), u) + b9, ou = mulq(p.q_o9, u);
-        f[5] = mulq(p.q_om1, f[5]) + sym + ou;
-        f[3] = mulq(p.q_om1, f[3]) + sym - ou;
+        const long long sym = mulc((unsigned long long)p.q_k9, jx2) + b9, ou = mulc((unsigned long long)p.q_o9, jx);
+        f[5] = f[5] + sym + ou - 2 * mulc(wh, f[5]);
+        f[3] = f[3] + sym - ou - 2 * mulc(wh, f[3]);
     }
     {
-        const long long u = jy, sym = mulq(mulq(p.q_k9, u), u) + b9, ou = mulq(p.q_o9, u);
-        f[7] = mulq(p.q_om1, f[7]) + sym + ou;
-        f[1] = mulq(p.q_om1, f[1]) + sym - ou;
+        const long long sym = mulc((unsigned long long)p.q_k9, jy2) + b9, ou = mulc((unsigned long long)p.q_o9, jy);
+        f[7] = f[7] + sym + ou - 2 * mulc(wh, f[7]);
+        f[1] = f[1] + sym - ou - 2 * mulc(wh, f[1]);
     }
     {
-        const long long u = jx + jy, sym = mulq(mulq(p.q_k36, u), u) + b36, ou = mulq(p.q_o36, u);
-        f[8] = mulq(p.q_om1, f[8]) + sym + ou;
-        f[0] = mulq(p.q_om1, f[0]) + sym - ou;
+        const long long sym = mulc((unsigned long long)p.q_k36, usq + 2 * jxy) + b36;
+        const long long ou = mulc((unsigned long long)p.q_o36, jx + jy);
+        f[8] = f[8] + sym + ou - 2 * mulc(wh, f[8]);
+        f[0] = f[0] + sym - ou - 2 * mulc(wh, f[0]);
     }
     {
-        const long long u = jx - jy, sym = mulq(mulq(p.q_k36, u), u) + b36, ou = mulq(p.q_o36, u);
-        f[2] = mulq(p.q_om1, f[2]) + sym + ou;
-        f[6] = mulq(p.q_om1, f[6]) + sym - ou;
+        const long long sym = mulc((unsigned long long)p.q_k36, usq - 2 * jxy) + b36;
+        const long long ou = mulc((unsigned long long)p.q_o36, jx - jy);
+        f[2] = f[2] + sym + ou - 2 * mulc(wh, f[2]);
+        f[6] = f[6] + sym - ou - 2 * mulc(wh, f[6]);
     }
-    unsigned long long bad = 0;
+    // populations in [-4, 4) and momenta in [-2, 2), or the status word is set
+    unsigned long long bad = (((unsigned long long)(jx + (1ll << 61))) | ((unsigned long long)(jy + (1ll << 61)))) >> 62;
 #pragma unroll
     for (int d = 0; d < 9; ++d) bad |= q_out_of_range(f[d]);
     if (bad) atomicOr(p.status, 1);
@@ -344,10 +371,10 @@ __device__ __forceinline__ void outlet_fill(typename Store<PREC>::C f[9], double
         f[6] = __dadd_rn(__dsub_rn(__dadd_rn(g2, hd), x6), hy);
     } else if constexpr (PREC == F64_Q60) {
         const long long xv = -p.q_rho_out + ((f[1] + f[4] + f[7]) + 2 * (f[8] + f[5] + f[2]));
-        const long long hd = (f[1] - f[7]) >> 1, x6 = mulq(p.q_sixth, xv), hy = double_to_q(jyo) >> 1;
+        const long long hd = (f[1] - f[7]) >> 1, x6 = mulc((unsigned long long)p.q_sixth, xv), hy = double_to_q(jyo) >> 1;
         const long long g0 = f[8], g1 = f[5], g2 = f[2];
         f[0] = g0 - hd - x6 - hy;
-        f[3] = g1 - mulq(p.q_two_thirds, xv);
+        f[3] = g1 - mulc((unsigned long long)p.q_two_thirds, xv);
         f[6] = g2 + hd - x6 + hy;
     } else if constexpr (PREC == F32_REF) {
         const float xv = __fadd_rn(-p.rho_outf,

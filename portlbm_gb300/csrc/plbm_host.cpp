@@ -383,8 +383,14 @@ int alg_index(const std::string &a) { return a == "nptl" ? 0 : a == "lptl" ? 1 :
 int layout_index(const std::string &l) { return l == "collision" ? 0 : l == "stream" ? 1 : 2; }
 size_t storage_bytes(int prec) { return (prec <= 1 || prec == PLBM_F64_Q60) ? 8 : prec <= 3 ? 4 : 2; }
 
-// round(x * 2^60) for the Q60 form's constants, evaluated in long double.
+// round(x * 2^60) (populations) and round(c * 2^64) for constants 0 <= c < 1, in long double.
 long long q60(long double x) { return (long long)std::llroundl(x * 1152921504606846976.0L); }
+long long q64(long double c)
+{
+    const long double v = c * 18446744073709551616.0L + 0.5L;
+    const unsigned long long u = v >= 18446744073709551615.0L ? 18446744073709551615ull : (unsigned long long)v;
+    return (long long)u;   // bit pattern of the unsigned Q0.64 value
+}
 
 thread_local std::string g_tls_error;
 std::mutex g_create_mu;
@@ -590,13 +596,13 @@ struct plbm_handler {
         {
             // Q60 constants from the reference's double constants (1/tau, w_d, 1.0/6, 2.0/3)
             const long double om = (long double)b.omega, w9 = 1.0 / 9, w36 = 1.0 / 36, w49 = 4.0 / 9;
-            b.q_om1 = q60(1.0L - om);
-            b.q_ow49 = q60(om * w49); b.q_ow9 = q60(om * w9); b.q_ow36 = q60(om * w36);
-            b.q_k9 = q60(4.5L * om * w9); b.q_k36 = q60(4.5L * om * w36);
-            b.q_o9 = q60(3.0L * om * w9); b.q_o36 = q60(3.0L * om * w36);
+            b.q_om1 = q64(om / 2);   // the Q60 kernel applies omega as twice omega/2
+            b.q_ow49 = q64(om * w49); b.q_ow9 = q64(om * w9); b.q_ow36 = q64(om * w36);
+            b.q_k9 = q64(4.5L * om * w9); b.q_k36 = q64(4.5L * om * w36);
+            b.q_o9 = q64(3.0L * om * w9); b.q_o36 = q64(3.0L * om * w36);
             b.q_rho_out = q60((long double)b.rho_out);
-            b.q_sixth = q60((long double)(1.0 / 6));
-            b.q_two_thirds = q60((long double)(2.0 / 3));
+            b.q_sixth = q64((long double)(1.0 / 6));
+            b.q_two_thirds = q64((long double)(2.0 / 3));
             for (int d = 0; d < 9; ++d) {
                 b.q_weight[d] = q60((long double)b.weight[d]);
                 b.q_feq_in[d] = q60((long double)b.feq_in[d]);
@@ -604,6 +610,8 @@ struct plbm_handler {
             }
             b.status = status_d;
             if (prec == PLBM_F64_Q60) {
+                if (!(props.tau > 0.5))
+                    fail(PLBM_ERR_NUMERIC, "f64_q60 needs relaxation_time > 0.5 (omega/2 below 1); use f64_strict");
                 for (int d = 0; d < 9; ++d)
                     if (std::fabs(b.feq_in[d]) >= 4 || std::fabs(b.feq_out[d]) >= 4)
                         fail(PLBM_ERR_NUMERIC, "f64_q60 needs boundary populations in [-4, 4); use f64_strict");

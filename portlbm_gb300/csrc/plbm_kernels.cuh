@@ -54,11 +54,15 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
         lk[j] = in ? p.links[n[j]] : 0;
     }
 #pragma unroll
-    for (int j = 0; j < NY; ++j)
-        if (lk[j] & LINK_FLUID) {
+    for (int j = 0; j < NY; ++j) {
+        if (interior_fluid(xi[j], yi[j], lk[j], p)) {
+#pragma unroll
+            for (int d = 0; d < 9; ++d) f[j][d] = ld<PREC>(p.lat0, lidx<L>(n[j], d, p.N) + pull_delta<L>(d, p), d, p);
+        } else if (lk[j] & LINK_FLUID) {
 #pragma unroll
             for (int d = 0; d < 9; ++d) f[j][d] = pull_one<PREC, L>(p.lat0, n[j], xi[j], yi[j], d, lk[j], p);
         }
+    }
 #pragma unroll
     for (int j = 0; j < NY; ++j) {
         if (!(lk[j] & LINK_FLUID)) continue;
@@ -189,28 +193,39 @@ __global__ void k_nsol_even(StepParams p)
     const uint16_t lk = p.links[n];
     if (!(lk & LINK_FLUID)) return;
     CT<PREC> f[9];
+    const bool fast = interior_fluid(xi, yi, lk, p);
+    if (fast) {
 #pragma unroll
-    for (int d = 0; d < 9; ++d) {
-        const int sx = xi - cxd(d), sy = yi - cyd(d);
-        if (d == 4) {
-            f[4] = ld<PREC>(p.lat0, lidx<L>(n, 4, p.N), 4, p);
-        } else if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H) {
-            f[d] = (sy < 0 || sy >= p.H) ? g_weight<PREC>(p, d) : (sx < 0 ? g_in<PREC>(p, d) : g_out<PREC>(p, d));
-        } else if (lk & (1u << d)) {
-            f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N), d, p);          // own post-collision 8-d
-        } else {
-            const unsigned long long s = (unsigned long long)sx + (unsigned long long)sy * p.P;
-            f[d] = ld<PREC>(p.lat0, lidx<L>(s, 8 - d, p.N), 8 - d, p);
+        for (int d = 0; d < 9; ++d) f[d] = ld<PREC>(p.lat0, lidx<L>(n, 8 - d, p.N) + pull_delta<L>(d, p), 8 - d, p);
+    } else {
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {
+            const int sx = xi - cxd(d), sy = yi - cyd(d);
+            if (d == 4) {
+                f[4] = ld<PREC>(p.lat0, lidx<L>(n, 4, p.N), 4, p);
+            } else if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H) {
+                f[d] = (sy < 0 || sy >= p.H) ? g_weight<PREC>(p, d) : (sx < 0 ? g_in<PREC>(p, d) : g_out<PREC>(p, d));
+            } else if (lk & (1u << d)) {
+                f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N), d, p);          // own post-collision 8-d
+            } else {
+                const unsigned long long s = (unsigned long long)sx + (unsigned long long)sy * p.P;
+                f[d] = ld<PREC>(p.lat0, lidx<L>(s, 8 - d, p.N), 8 - d, p);
+            }
         }
     }
     if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
     const Moments m = collide<PREC>(f, p);
+    if (fast) {
 #pragma unroll
-    for (int d = 0; d < 9; ++d) {
-        const int tx = xi + cxd(d), ty = yi + cyd(d);
-        if (tx < 0 || tx >= p.W || ty < 0 || ty >= p.H) continue;   // toward a ghost: never read
-        const unsigned long long t = (unsigned long long)tx + (unsigned long long)ty * p.P;
-        st<PREC>(p.lat0, lidx<L>(t, d, p.N), d, f[d], p);
+        for (int d = 0; d < 9; ++d) st<PREC>(p.lat0, lidx<L>(n, d, p.N) - pull_delta<L>(d, p), d, f[d], p);
+    } else {
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {
+            const int tx = xi + cxd(d), ty = yi + cyd(d);
+            if (tx < 0 || tx >= p.W || ty < 0 || ty >= p.H) continue;   // toward a ghost: never read
+            const unsigned long long t = (unsigned long long)tx + (unsigned long long)ty * p.P;
+            st<PREC>(p.lat0, lidx<L>(t, d, p.N), d, f[d], p);
+        }
     }
     observables<PREC>(m, xi, yi, p);
 }
@@ -225,18 +240,23 @@ __global__ void k_nsol_odd(StepParams p)
     const uint16_t lk = p.links[n];
     if (!(lk & LINK_FLUID)) return;
     CT<PREC> f[9];
+    if (interior_fluid(xi, yi, lk, p)) {
 #pragma unroll
-    for (int d = 0; d < 9; ++d) {
-        const int sx = xi - cxd(d), sy = yi - cyd(d);
-        if (d == 4) {
-            f[4] = ld<PREC>(p.lat0, lidx<L>(n, 4, p.N), 4, p);
-        } else if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H) {
-            f[d] = (sy < 0 || sy >= p.H) ? g_weight<PREC>(p, d) : (sx < 0 ? g_in<PREC>(p, d) : g_out<PREC>(p, d));
-        } else if (lk & (1u << d)) {
-            const unsigned long long s = (unsigned long long)sx + (unsigned long long)sy * p.P;
-            f[d] = ld<PREC>(p.lat0, lidx<L>(s, 8 - d, p.N), 8 - d, p);  // parked in the solid's slot
-        } else {
-            f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N), d, p);
+        for (int d = 0; d < 9; ++d) f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N), d, p);
+    } else {
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {
+            const int sx = xi - cxd(d), sy = yi - cyd(d);
+            if (d == 4) {
+                f[4] = ld<PREC>(p.lat0, lidx<L>(n, 4, p.N), 4, p);
+            } else if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H) {
+                f[d] = (sy < 0 || sy >= p.H) ? g_weight<PREC>(p, d) : (sx < 0 ? g_in<PREC>(p, d) : g_out<PREC>(p, d));
+            } else if (lk & (1u << d)) {
+                const unsigned long long s = (unsigned long long)sx + (unsigned long long)sy * p.P;
+                f[d] = ld<PREC>(p.lat0, lidx<L>(s, 8 - d, p.N), 8 - d, p);  // parked in the solid's slot
+            } else {
+                f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N), d, p);
+            }
         }
     }
     if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
