@@ -37,6 +37,21 @@ __device__ __forceinline__ CT<PREC> pull_one(const void *S, unsigned long long n
     return ld<PREC>(S, lidx<L>(s, d, p.N), d, p);
 }
 
+// Index offset from node n's entry of direction k to node (n + dn)'s entry of direction k, where
+// dn = -cx_d - cy_d * P is the pull source of direction d.
+template <int L>
+__device__ __forceinline__ long long pull_delta(int d, const StepParams &p)
+{
+    const long long dn = -(long long)cxd(d) - (long long)cyd(d) * p.P;
+    return L == COLLISION ? 9 * dn : (L == STREAM ? dn : 3 * dn);
+}
+
+// Nodes away from the domain edge whose eight sources are all fluid take no per-direction checks.
+__device__ __forceinline__ bool interior_fluid(int xi, int yi, uint16_t lk, const StepParams &p)
+{
+    return lk == LINK_FLUID && xi > 0 && xi < p.W - 1 && yi > 0 && yi < p.H - 1;
+}
+
 // Rows per thread: a node of the 2-byte forms moves only 36 B, so each thread issues the loads of
 // several nodes before computing any of them to keep enough bytes in flight per SM.
 template <int PREC> struct RowsPerThread { static constexpr int value = rows_per_thread(PREC); };
