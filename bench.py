@@ -5,8 +5,10 @@ obstacle of radius H/8 centred at (W/4, H/2), inlet density 1.2 / outlet 1.0, ta
 algorithm, stream layout.  A "step" is one lattice-Boltzmann timestep over the whole domain.
 
 * ``value``      MLUPS (W*H inner nodes x steps / s) of K device-resident steps, timed with CUDA
-                 events on the solver's stream; FP64 "fast" form (FMA-regrouped BGK, agrees with
-                 the reference to <= 1e-12, see tests/test_gpu_parity.py).
+                 events on the solver's stream, of the FP64-accuracy form f64_q60 (populations in
+                 64-bit fixed point, BGK update on the integer pipe; agrees with the reference to
+                 <= 1e-12, see tests/test_gpu_parity.py).  ``err_vs_oracle`` restates that error
+                 live: max |GPU - oracle| of rho, jx, jy after 2000 steps of the 400x100 channel.
 * ``e2e``        the same metric through the public API with host buffers: create_handler from
                  host properties + host mask (H2D), K steps, results read back (D2H), all timed.
 * ``roofline``   HBM roofline of the step kernel: 144 algorithmic bytes per node update (9 loads +
@@ -160,6 +162,23 @@ def cpu_oracle_sample(w, h, steps, mask, threads=None):
     return w * h * steps / dt / 1e6, plbm_oracle.threads(), dt
 
 
+def err_vs_oracle(plbm, precision, steps=2000, w=400, h=100):
+    """max |GPU - oracle| over rho, jx, jy for the 400x100 Hagen-Poiseuille channel."""
+    from oracle import plbm_oracle
+    plbm_oracle.build()
+    props = plbm.Properties("nptl", "stream", False, 1024, steps, steps, "Hagen-Poiseuille", h, w, 0.0, 0.0, 1.2,
+                            0.0, 0.0, 1.0, 0.6)
+    hd = plbm.create_handler(props, precision=precision)
+    hd.start()
+    hd.block_until_finished()
+    got = [hd.get_densities(), hd.get_x_velocities(), hd.get_y_velocities()]
+    hd.close()
+    o = plbm_oracle.Oracle("nptl", "stream", 1024, "Hagen-Poiseuille", w, h, inlet_density=1.2, relaxation_time=0.6)
+    o.run(steps)
+    ref = [o.result(0), o.result(1), o.result(2)]
+    return float(max(np.max(np.abs(a - b)) for a, b in zip(got, ref)))
+
+
 def load_traffic(kind: str):
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -239,7 +258,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--width", type=int, default=W_DEFAULT)
     ap.add_argument("--height", type=int, default=H_DEFAULT)
-    ap.add_argument("--precision", default="f64_fast", choices=list(BYTES_PER_NODE))
+    ap.add_argument("--precision", default="f64_q60", choices=list(BYTES_PER_NODE))
     ap.add_argument("--algorithm", default="nptl")
     ap.add_argument("--layout", default="stream")
     ap.add_argument("--no-variants", action="store_true")
@@ -287,7 +306,7 @@ def main():
     # -- other forms of the same step (device-resident, same K), reported beside --
     variants = {}
     if not args.no_variants and rank == 0:
-        for prec in ("f64_strict", "f32", "f16s", "bf16s"):
+        for prec in ("f64_strict", "f64_fast", "f32", "f16s", "bf16s"):
             if prec == args.precision:
                 continue
             vms, vh = device_run(plbm, prec, args.algorithm, args.layout, w, h, mask, max(20, args.steps // 4), 5)
@@ -295,6 +314,8 @@ def main():
             variants[prec] = {"mlups": round(w * h / vms / 1e3, 1), "ms_per_step": round(vms, 4),
                               "hbm_gbs": round(BYTES_PER_NODE[prec] * w * h / vms / 1e6, 1),
                               "frac_of_hbm": round(BYTES_PER_NODE[prec] * w * h / vms / 1e6 / pk["hbm_gbs"], 4)}
+
+    err = err_vs_oracle(plbm, args.precision) if rank == 0 else None
 
     # -- CPU baseline (rank 0, N = 1) --
     cpu = None
@@ -311,7 +332,8 @@ def main():
             "metric": "MLUPS (FP64 D2Q9 BGK, 8192x8192 circle channel)",
             "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
+            "dtype": "int64 (Q3.60 fixed point, FP64 accuracy)" if args.precision == "f64_q60" else "f64",
+            "data": "synthetic", "err_vs_oracle": err,
             "config": {"workload": f"circle channel {w}x{h} (r=H/8 at W/4), nptl+stream, tau 0.6, rho 1.2/1.0",
                        "algorithm": args.algorithm, "data_layout": args.layout, "precision": args.precision,
                        "l2": "inputs larger than L2 (lattice %.1f GB)" % (2 * 9 * 8 * w * h / 1e9),
@@ -319,7 +341,8 @@ def main():
             "roofline": {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                          "frac": round(achieved_gbs / pk["hbm_gbs"], 4), "traffic": traffic,
                          "peak_source": pk["source"],
-                         "note": "FP64 forms issue-bound on the FP64 pipe (0.5 T DP instr/s measured)"},
+                         "note": ("f64_strict/f64_fast are bound by the FP64 pipe (0.5 T DP instr/s measured); "
+                                  "f64_q60 runs the update on the integer pipe")},
             "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS", "h2d_bytes_per_step": round(w * h / e2e_steps),
                     "d2h_bytes_per_step": round(4 * 8 * w * h / e2e_steps)},
             "gpu_launches": launches,
