@@ -179,13 +179,15 @@ def err_vs_oracle(plbm, precision, steps=2000, w=400, h=100):
     return float(max(np.max(np.abs(a - b)) for a, b in zip(got, ref)))
 
 
-def load_traffic(kind: str):
-    p = os.path.join(ROOT, "profiles", "traffic.json")
-    try:
-        with open(p) as f:
-            return json.load(f).get(kind)
-    except Exception:
-        return None
+# DRAM bytes (read + write) per step launch from one ncu capture of the 4096 x 4096 circle channel
+# (profiles/k_nptl_f64q60_stream_4096x4096.md, profiles/k_nptl_f64fast_stream_4096x4096.md), per
+# node; traffic is proportional to the node count at fixed geometry, so the bench scales it.
+TRAFFIC_PER_NODE = {"nptl_stream_f64_q60": 2.283e9 / (4096 * 4096), "nptl_stream_f64_fast": 2.283e9 / (4096 * 4096)}
+
+
+def load_traffic(kind: str, nodes: int):
+    v = TRAFFIC_PER_NODE.get(kind)
+    return None if v is None else round(v * nodes)
 
 
 def dist_setup():
@@ -327,7 +329,7 @@ def main():
                          f"{dt:.1f} s)"}
 
     if rank == 0:
-        traffic = load_traffic(f"{args.algorithm}_{args.layout}_{args.precision}")
+        traffic = load_traffic(f"{args.algorithm}_{args.layout}_{args.precision}", w * h)
         line = {
             "metric": "MLUPS (FP64 D2Q9 BGK, 8192x8192 circle channel)",
             "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
