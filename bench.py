@@ -185,6 +185,57 @@ def err_vs_oracle(plbm, precision, steps=2000, w=400, h=100):
 TRAFFIC_PER_NODE = {"nptl_stream_f64_q60": 2.283e9 / (4096 * 4096), "nptl_stream_f64_fast": 2.283e9 / (4096 * 4096)}
 
 
+def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, max_steps=100000,
+                    big=(8192, 8192), big_steps=2000):
+    """Each storage form against the FP64 drop-in on a seeded porous channel (disks r in [3, 12],
+    tau 0.6, rho 1.01 / 1.0): steps to residual `target`, relative L2 error of the momentum field
+    and relative total-mass difference at steady state; then the same errors on the 8192^2 porous
+    channel after `big_steps` steps against f64_q60 (FP64 accuracy, <= 1e-12 from the drop-in)."""
+    mask = plbm.porous_disks(w, h, seed, porosity)
+    fluid = mask.reshape(-1) == 0
+
+    def run(prec, mk, ww, hh, to_residual=True, steps=0):
+        props = plbm.Properties("nptl", "stream", False, 1024, 10 ** 9, 10 ** 9, "Hagen-Poiseuille", hh, ww, 0.0,
+                                0.0, 1.01, 0.0, 0.0, 1.0, 0.6)
+        hd = plbm.create_handler(props, precision=prec, mask=mk)
+        t0 = time.perf_counter()
+        if to_residual:
+            n, r = hd.run_to_residual(target, 100, max_steps)
+        else:
+            hd.run_steps(steps)
+            hd.sync_results()
+            n, r = steps, None
+        dt = time.perf_counter() - t0
+        out = (hd.get_densities(), hd.get_x_velocities(), hd.get_y_velocities())
+        hd.close()
+        return n, r, dt, out
+
+    def errs(a, b, fl):
+        ja = np.concatenate([a[1][fl], a[2][fl]])
+        jb = np.concatenate([b[1][fl], b[2][fl]])
+        return (float(np.linalg.norm(ja - jb) / np.linalg.norm(jb)),
+                float((a[0][fl].sum() - b[0][fl].sum()) / b[0][fl].sum()))
+
+    n64, r64, t64, ref = run("f64_strict", mask, w, h)
+    study = {"domain": f"{w}x{h} porous (seed {seed}, porosity {porosity})", "target_residual": target,
+             "f64_strict": {"steps": n64, "residual": r64, "seconds": round(t64, 3)}}
+    for prec in ("f64_q60", "f64_fast", "f32", "f16s", "bf16s"):
+        n, r, dt, out = run(prec, mask, w, h)
+        l2, dm = errs(out, ref, fluid)
+        study[prec] = {"steps": n, "residual": r, "seconds": round(dt, 3), "rel_l2_j_vs_f64": l2,
+                       "mass_rel_diff_vs_f64": dm}
+    bw, bh = big
+    bmask = plbm.porous_disks(bw, bh, seed, porosity)
+    bfl = bmask.reshape(-1) == 0
+    _, _, _, bref = run("f64_q60", bmask, bw, bh, False, big_steps)
+    study["large"] = {"domain": f"{bw}x{bh} porous, {big_steps} steps, against f64_q60"}
+    for prec in ("f32", "f16s", "bf16s"):
+        _, _, _, out = run(prec, bmask, bw, bh, False, big_steps)
+        l2, dm = errs(out, bref, bfl)
+        study["large"][prec] = {"rel_l2_j": l2, "mass_rel_diff": dm}
+    return study
+
+
 def load_traffic(kind: str, nodes: int):
     v = TRAFFIC_PER_NODE.get(kind)
     return None if v is None else round(v * nodes)
@@ -266,6 +317,7 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--cpu-steps", type=int, default=0, help="CPU-baseline sample steps (0: auto)")
     ap.add_argument("--kernel-only", action="store_true", help="only the device-resident timed region (profiling)")
+    ap.add_argument("--no-study", action="store_true", help="skip the precision study")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -318,6 +370,7 @@ def main():
                               "frac_of_hbm": round(BYTES_PER_NODE[prec] * w * h / vms / 1e6 / pk["hbm_gbs"], 4)}
 
     err = err_vs_oracle(plbm, args.precision) if rank == 0 else None
+    study = precision_study(plbm) if (rank == 0 and not args.no_study and not args.no_variants) else None
 
     # -- CPU baseline (rank 0, N = 1) --
     cpu = None
@@ -351,6 +404,7 @@ def main():
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
             "variants": variants,
+            "precision_study": study,
         }
         print(json.dumps(line), flush=True)
 

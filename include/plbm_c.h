@@ -192,6 +192,21 @@ int plbm_nptl_steps_noalloc(const plbm_noalloc_args *args);
 /* Message of the last failed plbm_nptl_steps_noalloc call on this thread. */
 const char *plbm_noalloc_last_error(void);
 
+/* ---- steady state and synthetic geometry (no counterpart in the reference) -------------- */
+
+/* Runs the loop in chunks of K steps until the residual
+ *   r = ||j^n - j^(n-K)||_2 / (K ||j^n||_2)   over fluid nodes (FP64 reductions on the GPU)
+ * falls below `target` or `max_steps` is reached; writes the steps taken and the last residual.
+ * Results on the host are those of the last step. */
+int plbm_run_to_residual(plbm_handler *h, double target, unsigned K, unsigned max_steps, unsigned *steps,
+                         double *residual);
+/* Porous channel geometry: solid walls on the first and last inner rows plus non-overlapping disks
+ * (radius uniform in [rmin, rmax]) placed at seeded random positions until the fluid fraction of
+ * the interior drops to `porosity`.  out: W*H int8 (0 fluid, 1 solid).  Returns the disk count
+ * (>= 0) or a negative status. */
+int plbm_porous_disks(unsigned inner_w, unsigned inner_h, uint64_t seed, double porosity, double rmin, double rmax,
+                      int8_t *out);
+
 /* Last error message for h (or of the last failed create when h is NULL). */
 const char *plbm_last_error(const plbm_handler *h);
 const char *plbm_version(void);

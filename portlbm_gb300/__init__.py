@@ -27,6 +27,7 @@ __all__ = [
     "Properties", "create_handler", "AlgorithmHandler", "Exception", "PropertyArgumentException",
     "WaitException", "CudaException", "ParseException", "NoDeviceException", "PRECISIONS",
     "properties_to_json", "json_to_properties", "library_path", "load_library", "compute_domain", "make_flags",
+    "porous_disks",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -113,6 +114,10 @@ _SIGS = {
     "plbm_mass_momentum": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "plbm_compute_domain": (ctypes.c_int, [ctypes.POINTER(_CProps), ctypes.POINTER(ctypes.c_uint)]),
     "plbm_make_flags": (ctypes.c_int, [ctypes.POINTER(_CProps), ctypes.c_void_p]),
+    "plbm_run_to_residual": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_uint, ctypes.c_uint,
+                                            ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_double)]),
+    "plbm_porous_disks": (ctypes.c_int, [ctypes.c_uint, ctypes.c_uint, ctypes.c_uint64, ctypes.c_double,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
     "plbm_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "plbm_version": (ctypes.c_char_p, []),
 }
@@ -228,6 +233,16 @@ def make_flags(props: Properties) -> np.ndarray:
     c = props._c()
     out = np.empty((props.vertical_nodes - 2, props.horizontal_nodes - 2), dtype=np.int8)
     _check(load_library().plbm_make_flags(ctypes.byref(c), out.ctypes.data))
+    return out
+
+
+def porous_disks(w: int, h: int, seed: int, porosity: float, rmin: float = 3.0, rmax: float = 12.0) -> np.ndarray:
+    """Seeded porous channel: walls on the first/last inner row plus non-overlapping disks with radius
+    uniform in [rmin, rmax] until the interior's fluid fraction reaches `porosity`; (H, W) int8."""
+    out = np.empty((h, w), dtype=np.int8)
+    n = load_library().plbm_porous_disks(w, h, seed, porosity, rmin, rmax, out.ctypes.data)
+    if n < 0:
+        _check(n)
     return out
 
 
@@ -360,6 +375,12 @@ class AlgorithmHandler:
         out = (ctypes.c_double * 3)()
         self._call("plbm_mass_momentum", out)
         return tuple(out)
+
+    def run_to_residual(self, target: float = 1e-6, k: int = 100, max_steps: int = 1_000_000) -> tuple:
+        """Steps in chunks of k until ||j^n - j^(n-k)|| / (k ||j^n||) < target; returns (steps, residual)."""
+        steps, r = ctypes.c_uint(), ctypes.c_double()
+        self._call("plbm_run_to_residual", float(target), int(k), int(max_steps), ctypes.byref(steps), ctypes.byref(r))
+        return steps.value, r.value
 
     def bytes_per_node(self) -> float:
         v = ctypes.c_double()

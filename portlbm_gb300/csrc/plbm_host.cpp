@@ -423,6 +423,7 @@ struct plbm_handler {
     void *halo[2] = { nullptr, nullptr };
     double *red_d = nullptr;
     int *status_d = nullptr;
+    double *jprev_d = nullptr;   // 2 * W*H: j of the previous residual evaluation
     double *res_h[4] = { nullptr, nullptr, nullptr, nullptr };
     size_t nres = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -460,6 +461,8 @@ struct plbm_handler {
         if (jy_d) cudaFree(jy_d);
         if (red_d) cudaFree(red_d);
         if (status_d) cudaFree(status_d);
+        if (jprev_d) cudaFree(jprev_d);
+        jprev_d = nullptr;
         links = nullptr; flags_d = nullptr; jy_d = nullptr; red_d = nullptr; status_d = nullptr;
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -1008,6 +1011,97 @@ int plbm_run_steps(plbm_handler *h, unsigned n, double *ms_per_step)
         h->iteration = t0 + n;
         h->progress = (double)(t0 + n) / (double)h->props.time_steps;
     });
+}
+
+int plbm_run_to_residual(plbm_handler *h, double target, unsigned K, unsigned max_steps, unsigned *steps,
+                         double *residual)
+{
+    return guarded(h, [&] {
+        if (K == 0) fail(PLBM_ERR_ARGUMENT, "K must be >= 1");
+        if (!h->jprev_d) {
+            cuda_check(cudaMalloc(&h->jprev_d, 2 * h->nres * sizeof(double)), "cudaMalloc residual");
+            cuda_check(cudaMemsetAsync(h->jprev_d, 0, 2 * h->nres * sizeof(double), h->stream), "memset");
+        }
+        unsigned done = 0;
+        double r = INFINITY;
+        bool first = true;
+        while (done < max_steps) {
+            const unsigned n = std::min(K, max_steps - done);
+            double ms = 0;
+            const int rc = plbm_run_steps(h, n, &ms);
+            if (rc != PLBM_OK) throw Status{ rc, h->last_error };
+            done += n;
+            double sums[2] = { 0, 0 };
+            cuda_check(plbm::launch_residual(h->res_d[1], h->res_d[2], h->jprev_d, h->jprev_d + h->nres, h->flags_d,
+                                             h->nres, h->red_d, h->stream), "residual");
+            cuda_check(cudaMemcpyAsync(sums, h->red_d, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
+            cuda_check(cudaStreamSynchronize(h->stream), "residual");
+            if (!first && n == K) r = sums[1] > 0 ? std::sqrt(sums[0]) / ((double)K * std::sqrt(sums[1])) : INFINITY;
+            first = false;
+            if (r < target) break;
+        }
+        h->copy_results();
+        *steps = done;
+        *residual = r;
+    });
+}
+
+int plbm_porous_disks(unsigned inner_w, unsigned inner_h, uint64_t seed, double porosity, double rmin, double rmax,
+                      int8_t *out)
+{
+    int count = 0;
+    const int rc = guarded(nullptr, [&] {
+        if (inner_w < 2 || inner_h < 3 || !(porosity > 0 && porosity <= 1) || !(rmin > 0 && rmax >= rmin))
+            fail(PLBM_ERR_ARGUMENT, "invalid porous-disk parameters");
+        const int W = (int)inner_w, H = (int)inner_h;
+        std::vector<int8_t> m((size_t)W * H, 0);
+        for (int x = 0; x < W; ++x) { m[x] = 1; m[(size_t)(H - 1) * W + x] = 1; }
+        // splitmix64 stream
+        uint64_t st = seed;
+        auto next = [&st]() {
+            uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            return z ^ (z >> 31);
+        };
+        auto uni = [&]() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); };
+        // spatial hash of placed disks on cells of 2*rmax
+        const double cell = 2 * rmax;
+        const int gx = (int)(W / cell) + 1, gy = (int)(H / cell) + 1;
+        std::vector<std::vector<int>> grid((size_t)gx * gy);
+        std::vector<double> cx, cy, cr;
+        const double interior = (double)W * (H - 2);
+        double solid = 0;
+        const double target = (1 - porosity) * interior;
+        long attempts = 0;
+        const long max_attempts = 200 * (long)(interior / (3.14159 * rmin * rmin) + 10);
+        while (solid < target && attempts < max_attempts) {
+            ++attempts;
+            const double r = rmin + (rmax - rmin) * uni();
+            const double x = uni() * W, y = 1 + r + uni() * (H - 2 - 2 * r);
+            const int ix = (int)(x / cell), iy = (int)(y / cell);
+            bool ok = true;
+            for (int ny = std::max(0, iy - 1); ny <= std::min(gy - 1, iy + 1) && ok; ++ny)
+                for (int nx = std::max(0, ix - 1); nx <= std::min(gx - 1, ix + 1) && ok; ++nx)
+                    for (int k : grid[(size_t)ny * gx + nx]) {
+                        const double dx = cx[k] - x, dy = cy[k] - y, rr = cr[k] + r + 1;
+                        if (dx * dx + dy * dy < rr * rr) { ok = false; break; }
+                    }
+            if (!ok) continue;
+            const int k = (int)cx.size();
+            cx.push_back(x); cy.push_back(y); cr.push_back(r);
+            grid[(size_t)iy * gx + ix].push_back(k);
+            for (int py = std::max(1, (int)(y - r)); py <= std::min(H - 2, (int)(y + r) + 1); ++py)
+                for (int px = std::max(0, (int)(x - r)); px <= std::min(W - 1, (int)(x + r) + 1); ++px) {
+                    const double dx = px + 0.5 - x, dy = py + 0.5 - y;
+                    int8_t &c = m[(size_t)py * W + px];
+                    if (c == 0 && dx * dx + dy * dy <= r * r) { c = 1; solid += 1; }
+                }
+        }
+        std::memcpy(out, m.data(), m.size());
+        count = (int)cx.size();
+    });
+    return rc == PLBM_OK ? count : rc;
 }
 
 int plbm_sync_results(plbm_handler *h)

@@ -21,6 +21,9 @@ cudaError_t launch_fill_results(double *rho, double *jx, double *jy, double *ja,
 // FP64 sums over fluid nodes of the result arrays: out3 = {sum rho, sum jx, sum jy}.
 cudaError_t launch_reduce_results(const double *rho, const double *jx, const double *jy, const int8_t *flags,
                                   unsigned long long n, double *out3_dev, cudaStream_t s);
+// FP64 sums over fluid nodes: out2 = {sum |j - j_prev|^2, sum |j|^2}; then j_prev = j.
+cudaError_t launch_residual(const double *jx, const double *jy, double *jx_prev, double *jy_prev, const int8_t *flags,
+                            unsigned long long n, double *out2_dev, cudaStream_t s);
 int max_threads_for(int alg, int prec, int lay);
 
 }  // namespace plbm

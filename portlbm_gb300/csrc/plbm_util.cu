@@ -160,4 +160,46 @@ cudaError_t launch_reduce_results(const double *rho, const double *jx, const dou
     return cudaGetLastError();
 }
 
+__global__ void k_residual(const double *jx, const double *jy, double *jxp, double *jyp, const int8_t *flags,
+                           unsigned long long n, double *out)
+{
+    double a = 0, b = 0;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        if (flags[i] != 0) continue;
+        const double x = jx[i], y = jy[i], dx = x - jxp[i], dy = y - jyp[i];
+        a += dx * dx + dy * dy;
+        b += x * x + y * y;
+        jxp[i] = x;
+        jyp[i] = y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    __shared__ double sm[2][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { sm[0][wid] = a; sm[1][wid] = b; }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        a = lane < nw ? sm[0][lane] : 0;
+        b = lane < nw ? sm[1][lane] : 0;
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            b += __shfl_down_sync(0xffffffffu, b, o);
+        }
+        if (lane == 0) { atomicAdd(&out[0], a); atomicAdd(&out[1], b); }
+    }
+}
+
+cudaError_t launch_residual(const double *jx, const double *jy, double *jx_prev, double *jy_prev, const int8_t *flags,
+                            unsigned long long n, double *out2, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(out2, 0, 2 * sizeof(double), s);
+    if (e != cudaSuccess) return e;
+    k_residual<<<152 * 2, 256, 0, s>>>(jx, jy, jx_prev, jy_prev, flags, n, out2);
+    return cudaGetLastError();
+}
+
 }  // namespace plbm

@@ -120,3 +120,16 @@ def test_gpu_matches_reference_golden(plbm, case):
     for k in ("rho", "jx", "jy", "jabs"):
         ref = _ARRAYS[f"{case['name']}__{k}"]
         assert np.array_equal(got[k], ref), f"{k}: max abs {np.max(np.abs(got[k] - ref))}"
+
+
+def test_residual_decreases_and_steady_state_is_reached(plbm):
+    """run_to_residual: a 128x48 porous channel reaches residual 1e-6, and the momentum it reports
+    equals the momentum of the last step."""
+    mask = plbm.porous_disks(128, 48, 3, 0.7)
+    props = plbm.Properties("nptl", "stream", False, 64, 10 ** 6, 10 ** 6, "Hagen-Poiseuille", 48, 128, 0.0, 0.0,
+                            1.01, 0.0, 0.0, 1.0, 0.6)
+    hd = plbm.create_handler(props, precision="f64_q60", mask=mask)
+    steps, r = hd.run_to_residual(1e-6, 100, 200000)
+    assert r < 1e-6 and steps < 200000
+    jx = hd.get_x_velocities()
+    assert np.all(np.isfinite(jx)) and jx[mask.reshape(-1) == 0].mean() > 0

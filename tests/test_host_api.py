@@ -165,3 +165,12 @@ def test_flags_match_oracle(plbm, oracle_mod, sc):
 def test_create_without_gpu_fails_loudly(plbm):
     with pytest.raises(plbm.NoDeviceException):
         plbm.create_handler(P(plbm))
+
+
+def test_porous_disks_generator(plbm):
+    m = plbm.porous_disks(300, 120, 5, 0.7)
+    assert m.shape == (120, 300)
+    assert np.all(m[0] == 1) and np.all(m[-1] == 1)
+    assert abs((1 - m[1:-1].mean()) - 0.7) < 0.01
+    assert np.array_equal(m, plbm.porous_disks(300, 120, 5, 0.7))      # seeded
+    assert not np.array_equal(m, plbm.porous_disks(300, 120, 6, 0.7))
