@@ -51,16 +51,21 @@ template <> struct Store<F16S> { using T = __half; using C = float; };
 template <> struct Store<BF16S> { using T = __nv_bfloat16; using C = float; };
 template <> struct Store<F64_Q60> { using T = long long; using C = long long; };
 
-// Loads / stores between storage and compute type.  The FP16/BF16 forms store f - w_d * rho0
-// (rho0 = 1), which keeps the stored magnitudes small and the rounding error relative to the
-// deviation from rest rather than to f itself.
+// The FP32 / FP16 / BF16 forms hold every population as its deviation from rest,
+// df = f - w_d * rho0 (rho0 = 1), in storage AND in the collision: the BGK update is linear in
+// the rest part (feq_d - w_d = w_d (drho + 3 cu + 4.5 cu^2 - 1.5 u^2) with rho = 1 + drho), so the
+// same arithmetic applied to df yields df'.  Rounding then scales with the deviation from rest,
+// not with f itself.
+template <int PREC> constexpr bool shifted() { return PREC == F32 || PREC == F16S || PREC == BF16S; }
+
 template <int PREC>
 __device__ __forceinline__ typename Store<PREC>::C ld(const void *base, unsigned long long i, int d, const StepParams &p)
 {
     using T = typename Store<PREC>::T;
     const T *b = static_cast<const T *>(base);
-    if constexpr (PREC == F16S) return __half2float(b[i]) + p.weightf[d];
-    else if constexpr (PREC == BF16S) return __bfloat162float(b[i]) + p.weightf[d];
+    (void)d; (void)p;
+    if constexpr (PREC == F16S) return __half2float(b[i]);
+    else if constexpr (PREC == BF16S) return __bfloat162float(b[i]);
     else return b[i];
 }
 
@@ -69,8 +74,9 @@ __device__ __forceinline__ void st(void *base, unsigned long long i, int d, type
 {
     using T = typename Store<PREC>::T;
     T *b = static_cast<T *>(base);
-    if constexpr (PREC == F16S) b[i] = __float2half_rn(v - p.weightf[d]);
-    else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(v - p.weightf[d]);
+    (void)d; (void)p;
+    if constexpr (PREC == F16S) b[i] = __float2half_rn(v);
+    else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(v);
     else b[i] = v;
 }
 
@@ -451,6 +457,9 @@ __device__ __forceinline__ void observables(const Moments &m, int xi, int yi, co
         if (!p.write_results && xi != p.W - 2) return;
         const Moments d = { q_to_double(__double_as_longlong(m.rho)), q_to_double(__double_as_longlong(m.jx)),
                             q_to_double(__double_as_longlong(m.jy)), q_to_double(__double_as_longlong(m.usq)) };
+        write_observables(d, xi, yi, p);
+    } else if constexpr (shifted<PREC>()) {
+        const Moments d = { 1.0 + m.rho, m.jx, m.jy, m.usq };   // rho = 1 + drho
         write_observables(d, xi, yi, p);
     } else {
         write_observables(m, xi, yi, p);

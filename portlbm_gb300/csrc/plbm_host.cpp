@@ -589,13 +589,16 @@ struct plbm_handler {
             b.omega = (double)(1 / (float)props.tau);
             b.rho_out = (double)(float)props.orho;
         }
+        const bool shifted = prec == PLBM_F32 || prec == PLBM_F16S || prec == PLBM_BF16S;
         for (int d = 0; d < 9; ++d) {
-            b.weightf[d] = (float)b.weight[d];
-            b.feq_inf[d] = (float)b.feq_in[d];
-            b.feq_outf[d] = (float)b.feq_out[d];
+            // the shifted forms keep deviations from the rest state: ghosts are feq - w, rest is 0
+            b.weightf[d] = shifted ? 0.0f : (float)b.weight[d];
+            b.feq_inf[d] = shifted ? (float)(b.feq_in[d] - b.weight[d]) : (float)b.feq_in[d];
+            b.feq_outf[d] = shifted ? (float)(b.feq_out[d] - b.weight[d]) : (float)b.feq_out[d];
         }
         b.omegaf = (float)b.omega;
-        b.rho_outf = (float)b.rho_out;
+        // outlet: f1+f4+f7+2(f8+f5+f2) carries exactly 1 in rest weights, so xv = (1 - rho_out) + sum(df)
+        b.rho_outf = shifted ? (float)(b.rho_out - 1.0) : (float)b.rho_out;
         {
             // Q60 constants from the reference's double constants (1/tau, w_d, 1.0/6, 2.0/3)
             const long double om = (long double)b.omega, w9 = 1.0 / 9, w36 = 1.0 / 36, w49 = 4.0 / 9;
@@ -620,8 +623,10 @@ struct plbm_handler {
                         fail(PLBM_ERR_NUMERIC, "f64_q60 needs boundary populations in [-4, 4); use f64_strict");
             }
         }
+        double rest[9];
+        for (int d = 0; d < 9; ++d) rest[d] = shifted ? 0.0 : b.weight[d];
         for (int i = 0; i < (two_lattice() ? 2 : 1); ++i)
-            cuda_check(plbm::launch_fill_lattice(lat[i], prec, lay, N, b.weight, stream), "lattice fill");
+            cuda_check(plbm::launch_fill_lattice(lat[i], prec, lay, N, rest, stream), "lattice fill");
 
         b.links = links;
         b.rho = res_d[0]; b.jx = res_d[1]; b.jy = res_d[2]; b.jabs = res_d[3];
@@ -658,7 +663,7 @@ struct plbm_handler {
             const size_t hn = (size_t)b.n_col_bounds * H * 6 + (size_t)b.n_row_bounds * W * 6;
             for (auto &hp : halo) {
                 cuda_check(cudaMalloc(&hp, std::max<size_t>(hn, 1) * eb), "cudaMalloc halo");
-                cuda_check(plbm::launch_fill_halo(hp, prec, W, H, b.n_col_bounds, b.n_row_bounds, b.weight, stream),
+                cuda_check(plbm::launch_fill_halo(hp, prec, W, H, b.n_col_bounds, b.n_row_bounds, rest, stream),
                            "halo fill");
             }
         }
