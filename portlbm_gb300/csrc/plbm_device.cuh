@@ -56,7 +56,7 @@ template <> struct Store<F64_Q60> { using T = long long; using C = long long; };
 // the rest part (feq_d - w_d = w_d (drho + 3 cu + 4.5 cu^2 - 1.5 u^2) with rho = 1 + drho), so the
 // same arithmetic applied to df yields df'.  Rounding then scales with the deviation from rest,
 // not with f itself.
-template <int PREC> constexpr bool shifted() { return PREC == F32 || PREC == F16S || PREC == BF16S; }
+template <int PREC> __host__ __device__ constexpr bool shifted() { return PREC == F32 || PREC == F16S || PREC == BF16S; }
 
 template <int PREC>
 __device__ __forceinline__ typename Store<PREC>::C ld(const void *base, unsigned long long i, int d, const StepParams &p)
