@@ -207,6 +207,35 @@ int plbm_run_to_residual(plbm_handler *h, double target, unsigned K, unsigned ma
 int plbm_porous_disks(unsigned inner_w, unsigned inner_h, uint64_t seed, double porosity, double rmin, double rmax,
                       int8_t *out);
 
+/* ---- batches of independent domains (no counterpart in the reference) ------------------
+ * Many channels of different sizes, relaxation times and inlet densities advanced together:
+ * PLBM_BATCH_PERSISTENT runs one persistent launch per step whose blocks take tiles of every
+ * domain from a shared work queue; PLBM_BATCH_PERSISTENT_GRAPH replays runs of those steps from a
+ * captured CUDA graph; PLBM_BATCH_PER_DOMAIN launches one kernel per domain per step (the
+ * comparison).  Each domain is a channel with its own W x H mask (0 fluid, 1 solid; copied),
+ * zero inlet/outlet velocity; nptl update, stream layout.  Precisions: PLBM_F32, PLBM_F16S,
+ * PLBM_BF16S, PLBM_F64_Q60. */
+typedef struct plbm_batch plbm_batch;
+typedef struct {
+    unsigned inner_w, inner_h;
+    double relaxation_time, inlet_density, outlet_density;
+    const int8_t *mask;
+} plbm_batch_domain;
+enum { PLBM_BATCH_PERSISTENT = 0, PLBM_BATCH_PERSISTENT_GRAPH = 1, PLBM_BATCH_PER_DOMAIN = 2 };
+
+int plbm_batch_create(unsigned n, const plbm_batch_domain *domains, int precision, plbm_batch **out);
+void plbm_batch_destroy(plbm_batch *b);
+/* Tile shape (threads of one block) and resident blocks per SM of the persistent launch. */
+int plbm_batch_set_tile(plbm_batch *b, int tile_w, int tile_h, int blocks_per_sm);
+/* Times `steps` persistent steps for each candidate tile shape and occupancy, keeps the fastest
+ * (the timed steps advance the batch). */
+int plbm_batch_autotune(plbm_batch *b, unsigned steps, int *tile_w, int *tile_h, int *blocks_per_sm);
+/* Advances every domain by `steps`; results are written on the last one.  Device ms per step. */
+int plbm_batch_run(plbm_batch *b, unsigned steps, int mode, double *ms_per_step);
+int plbm_batch_results(plbm_batch *b, unsigned domain, int which, double *out);
+int plbm_batch_info(plbm_batch *b, unsigned long long *nodes, unsigned *tiles);
+const char *plbm_batch_last_error(void);
+
 /* Last error message for h (or of the last failed create when h is NULL). */
 const char *plbm_last_error(const plbm_handler *h);
 const char *plbm_version(void);

@@ -27,7 +27,7 @@ __all__ = [
     "Properties", "create_handler", "AlgorithmHandler", "Exception", "PropertyArgumentException",
     "WaitException", "CudaException", "ParseException", "NoDeviceException", "PRECISIONS",
     "properties_to_json", "json_to_properties", "library_path", "load_library", "compute_domain", "make_flags",
-    "porous_disks",
+    "porous_disks", "Batch",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -391,6 +391,85 @@ class AlgorithmHandler:
         v = ctypes.c_uint()
         self._call("plbm_launches_per_step", ctypes.byref(v))
         return v.value
+
+
+class _CBatchDomain(ctypes.Structure):
+    _fields_ = [("inner_w", ctypes.c_uint), ("inner_h", ctypes.c_uint), ("relaxation_time", ctypes.c_double),
+                ("inlet_density", ctypes.c_double), ("outlet_density", ctypes.c_double), ("mask", ctypes.c_void_p)]
+
+
+BATCH_MODES = {"persistent": 0, "persistent_graph": 1, "per_domain": 2}
+
+
+class Batch:
+    """Many independent channels advanced together (plbm_batch_* in include/plbm_c.h)."""
+
+    def __init__(self, domains, precision: str = "f32"):
+        """domains: iterable of dicts {mask: (H, W) int8, relaxation_time, inlet_density, outlet_density}."""
+        lib = load_library()
+        self._lib = lib
+        for name, res, args in (
+                ("plbm_batch_create", ctypes.c_int, [ctypes.c_uint, ctypes.POINTER(_CBatchDomain), ctypes.c_int,
+                                                     ctypes.POINTER(ctypes.c_void_p)]),
+                ("plbm_batch_destroy", None, [ctypes.c_void_p]),
+                ("plbm_batch_set_tile", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+                ("plbm_batch_autotune", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint] + [ctypes.POINTER(ctypes.c_int)] * 3),
+                ("plbm_batch_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint, ctypes.c_int,
+                                                  ctypes.POINTER(ctypes.c_double)]),
+                ("plbm_batch_results", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint, ctypes.c_int, ctypes.c_void_p]),
+                ("plbm_batch_info", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_ulonglong),
+                                                   ctypes.POINTER(ctypes.c_uint)]),
+                ("plbm_batch_last_error", ctypes.c_char_p, [])):
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        self._masks = [np.ascontiguousarray(d["mask"], dtype=np.int8) for d in domains]
+        arr = (_CBatchDomain * len(self._masks))()
+        self.shapes = []
+        for i, (d, m) in enumerate(zip(domains, self._masks)):
+            arr[i] = _CBatchDomain(m.shape[1], m.shape[0], d["relaxation_time"], d["inlet_density"],
+                                   d.get("outlet_density", 1.0), m.ctypes.data)
+            self.shapes.append(m.shape)
+        h = ctypes.c_void_p()
+        rc = lib.plbm_batch_create(len(self._masks), arr, PRECISIONS[precision], ctypes.byref(h))
+        if rc != 0:
+            raise _CODES.get(rc, Exception)(lib.plbm_batch_last_error().decode())
+        self._h = h
+
+    def _ok(self, rc):
+        if rc != 0:
+            raise _CODES.get(rc, Exception)(self._lib.plbm_batch_last_error().decode())
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.plbm_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def set_tile(self, tile_w: int, tile_h: int, blocks_per_sm: int = 8):
+        self._ok(self._lib.plbm_batch_set_tile(self._h, tile_w, tile_h, blocks_per_sm))
+
+    def autotune(self, steps: int = 4) -> tuple:
+        w, h, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._ok(self._lib.plbm_batch_autotune(self._h, steps, ctypes.byref(w), ctypes.byref(h), ctypes.byref(b)))
+        return w.value, h.value, b.value
+
+    def run(self, steps: int, mode: str = "persistent_graph") -> float:
+        ms = ctypes.c_double()
+        self._ok(self._lib.plbm_batch_run(self._h, steps, BATCH_MODES[mode], ctypes.byref(ms)))
+        return ms.value
+
+    def result(self, domain: int, which: int) -> np.ndarray:
+        h, w = self.shapes[domain]
+        out = np.empty(h * w, dtype=np.float64)
+        self._ok(self._lib.plbm_batch_results(self._h, domain, which, out.ctypes.data))
+        return out
+
+    def info(self) -> tuple:
+        n, t = ctypes.c_ulonglong(), ctypes.c_uint()
+        self._ok(self._lib.plbm_batch_info(self._h, ctypes.byref(n), ctypes.byref(t)))
+        return n.value, t.value
 
 
 def create_handler(source, precision: str = "f64_strict", mask=None, nan_protection: bool = True,

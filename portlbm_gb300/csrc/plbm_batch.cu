@@ -1,0 +1,433 @@
+// plbm_batch.cu — many independent domains advanced together: one persistent launch per timestep
+// walks a queue of tiles drawn from every domain (atomic ticket counter, reset by a memset node),
+// and runs of steps are replayed from a captured CUDA graph.  Each domain keeps its own two
+// lattices (stream layout), links, geometry, relaxation time and boundary densities; the per-node
+// update is the nptl update of plbm_kernels.cuh (FP32 or FP16 shifted storage, or F64_Q60).
+//
+// There is no counterpart in the reference, which runs one domain per handler; this is the
+// "batching" addition of the GB300 build.
+#include "../../include/plbm_c.h"
+#include "plbm_kernels.cuh"
+#include "plbm_launch.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace plbm {
+
+struct BatchArgs {
+    const StepParams *params;      // two per domain: parity 0 and 1
+    const unsigned *tile_domain;   // domain of each global tile
+    const unsigned *tile_local;    // tile index inside its domain
+    const int *tiles_x;            // tiles per row of each domain
+    unsigned n_tiles;
+    unsigned *ticket;              // work-queue counter, zeroed before every step
+    int tile_w, tile_h;
+    unsigned parity;
+    int write_results;
+};
+
+// Copies one StepParams into shared memory with the whole block, 8 bytes per thread per pass.
+__device__ __forceinline__ void stage_params(StepParams &dst, const StepParams &src)
+{
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+    unsigned long long *d = reinterpret_cast<unsigned long long *>(&dst);
+    const unsigned long long *s = reinterpret_cast<const unsigned long long *>(&src);
+    for (int i = tid; i < (int)(sizeof(StepParams) / 8); i += nt) d[i] = s[i];
+}
+
+// Persistent: every block takes tiles from the queue until it is empty; the tile's domain
+// parameters are staged in shared memory.
+template <int PREC>
+__global__ void k_batch(BatchArgs a)
+{
+    __shared__ __align__(16) StepParams sp;
+    __shared__ unsigned s_tile, s_dom;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    unsigned cur = 0xffffffffu;
+    for (;;) {
+        if (tid == 0) {
+            s_tile = atomicAdd(a.ticket, 1u);
+            s_dom = s_tile < a.n_tiles ? a.tile_domain[s_tile] : 0u;
+        }
+        __syncthreads();
+        const unsigned t = s_tile, dom = s_dom;
+        if (t >= a.n_tiles) return;
+        if (dom != cur) {
+            stage_params(sp, a.params[2 * dom + a.parity]);
+            __syncthreads();
+            if (tid == 0) sp.write_results = a.write_results;
+            cur = dom;
+        }
+        __syncthreads();
+        const int local = (int)a.tile_local[t], txs = a.tiles_x[dom];
+        const int xi = (local % txs) * a.tile_w + threadIdx.x, yi = (local / txs) * a.tile_h + threadIdx.y;
+        if (xi < sp.W && yi < sp.H) {
+            const int xs[1] = { xi }, ys[1] = { yi };
+            update_two_lattice_rows<PREC, STREAM, 1>(xs, ys, sp);
+        }
+        __syncthreads();   // s_tile / s_dom are rewritten for the next tile
+    }
+}
+
+// One launch per domain (the comparison the batching form is measured against).
+template <int PREC>
+__global__ void k_batch_single(BatchArgs a, unsigned domain)
+{
+    __shared__ __align__(16) StepParams sp;
+    stage_params(sp, a.params[2 * domain + a.parity]);
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) sp.write_results = a.write_results;
+    __syncthreads();
+    const int xi = blockIdx.x * blockDim.x + threadIdx.x, yi = blockIdx.y * blockDim.y + threadIdx.y;
+    if (xi < sp.W && yi < sp.H) {
+        const int xs[1] = { xi }, ys[1] = { yi };
+        update_two_lattice_rows<PREC, STREAM, 1>(xs, ys, sp);
+    }
+}
+
+}  // namespace plbm
+
+namespace {
+
+using plbm::StepParams;
+
+long long q60(long double x) { return (long long)std::llroundl(x * 1152921504606846976.0L); }
+long long q64(long double c)
+{
+    const long double v = c * 18446744073709551616.0L + 0.5L;
+    return (long long)(v >= 18446744073709551615.0L ? 18446744073709551615ull : (unsigned long long)v);
+}
+
+void mb(double ux, double uy, double rho, double *t)
+{
+    static const double w[9] = { 1.0 / 36, 1.0 / 9, 1.0 / 36, 1.0 / 9, 4.0 / 9, 1.0 / 9, 1.0 / 36, 1.0 / 9, 1.0 / 36 };
+    for (int d = 0; d < 9; ++d) {
+        const int vx = (d % 3) - 1, vy = (d / 3) - 1;
+        t[d] = w[d] * (rho + 3 * (vx * ux + vy * uy) + 9.0 / 2 * std::pow(vx * ux + vy * uy, 2) - 3.0 / 2 * (ux * ux + uy * uy));
+    }
+}
+
+}  // namespace
+
+struct plbm_batch {
+    int prec = PLBM_F32;
+    std::vector<StepParams> host;   // parity 0 and 1 per domain
+    std::vector<void *> allocs;
+    StepParams *dom_d = nullptr;
+    unsigned *tile_domain_d = nullptr, *tile_local_d = nullptr, *ticket_d = nullptr;
+    int *tiles_x_d = nullptr;
+    int *status_d = nullptr, *status_pending = nullptr;
+    unsigned n_tiles = 0, t = 0;
+    int tile_w = 32, tile_h = 4, blocks = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    unsigned graph_steps = 0;
+    std::string err;
+    unsigned long long nodes = 0;
+    std::vector<unsigned> tile_domain_host;
+
+    ~plbm_batch()
+    {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        for (void *p : allocs) cudaFree(p);
+        if (dom_d) cudaFree(dom_d);
+        if (tile_domain_d) cudaFree(tile_domain_d);
+        if (tile_local_d) cudaFree(tile_local_d);
+        if (tiles_x_d) cudaFree(tiles_x_d);
+        if (ticket_d) cudaFree(ticket_d);
+        if (status_pending) cudaFree(status_pending);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    unsigned n_domains() const { return (unsigned)(host.size() / 2); }
+
+    // Tiles of every domain in domain order; the queue hands them out in that order.
+    cudaError_t build_tiles()
+    {
+        std::vector<unsigned> dom, loc;
+        std::vector<int> tx;
+        for (unsigned i = 0; i < n_domains(); ++i) {
+            const StepParams &d = host[2 * i];
+            const int nx = (d.W + tile_w - 1) / tile_w, ny = (d.H + tile_h - 1) / tile_h;
+            tx.push_back(nx);
+            for (int k = 0; k < nx * ny; ++k) { dom.push_back(i); loc.push_back((unsigned)k); }
+        }
+        n_tiles = (unsigned)dom.size();
+        for (unsigned *p : { tile_domain_d, tile_local_d }) if (p) cudaFree(p);
+        if (tiles_x_d) cudaFree(tiles_x_d);
+        cudaError_t e = cudaMalloc(&tile_domain_d, n_tiles * sizeof(unsigned));
+        if (e == cudaSuccess) e = cudaMalloc(&tile_local_d, n_tiles * sizeof(unsigned));
+        if (e == cudaSuccess) e = cudaMalloc(&tiles_x_d, tx.size() * sizeof(int));
+        if (e == cudaSuccess) e = cudaMemcpyAsync(tile_domain_d, dom.data(), n_tiles * 4, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(tile_local_d, loc.data(), n_tiles * 4, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(tiles_x_d, tx.data(), tx.size() * 4, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        return e;
+    }
+
+    plbm::BatchArgs args(unsigned parity, int write_results) const
+    {
+        return plbm::BatchArgs{ dom_d, tile_domain_d, tile_local_d, tiles_x_d, n_tiles, ticket_d,
+                                tile_w, tile_h, parity, write_results };
+    }
+
+    cudaError_t launch(unsigned step, int write_results)
+    {
+        cudaError_t e = cudaMemsetAsync(ticket_d, 0, sizeof(unsigned), stream);
+        if (e != cudaSuccess) return e;
+        const plbm::BatchArgs a = args(step & 1u, write_results);
+        const dim3 block(tile_w, tile_h);
+        switch (prec) {
+        case PLBM_F32: plbm::k_batch<plbm::F32><<<blocks, block, 0, stream>>>(a); break;
+        case PLBM_F16S: plbm::k_batch<plbm::F16S><<<blocks, block, 0, stream>>>(a); break;
+        case PLBM_BF16S: plbm::k_batch<plbm::BF16S><<<blocks, block, 0, stream>>>(a); break;
+        default: plbm::k_batch<plbm::F64_Q60><<<blocks, block, 0, stream>>>(a); break;
+        }
+        return cudaGetLastError();
+    }
+
+    cudaError_t launch_per_domain(unsigned step, int write_results)
+    {
+        const plbm::BatchArgs a = args(step & 1u, write_results);
+        const dim3 block(32, 4);
+        for (unsigned i = 0; i < n_domains(); ++i) {
+            const dim3 grid((host[2 * i].W + 31) / 32, (host[2 * i].H + 3) / 4);
+            switch (prec) {
+            case PLBM_F32: plbm::k_batch_single<plbm::F32><<<grid, block, 0, stream>>>(a, i); break;
+            case PLBM_F16S: plbm::k_batch_single<plbm::F16S><<<grid, block, 0, stream>>>(a, i); break;
+            case PLBM_BF16S: plbm::k_batch_single<plbm::BF16S><<<grid, block, 0, stream>>>(a, i); break;
+            default: plbm::k_batch_single<plbm::F64_Q60><<<grid, block, 0, stream>>>(a, i); break;
+            }
+        }
+        return cudaGetLastError();
+    }
+
+    cudaError_t ensure_graph(unsigned steps_per_graph)
+    {
+        if (gexec && graph_steps == steps_per_graph) return cudaSuccess;
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        cudaError_t el = cudaSuccess;
+        for (unsigned k = 0; k < steps_per_graph && el == cudaSuccess; ++k) el = launch(k, 0);
+        e = cudaStreamEndCapture(stream, &g);
+        if (el != cudaSuccess) return el;
+        if (e != cudaSuccess) return e;
+        e = cudaGraphInstantiate(&gexec, g, 0);
+        cudaGraphDestroy(g);
+        graph_steps = steps_per_graph;
+        return e;
+    }
+};
+
+namespace {
+thread_local std::string g_batch_err;
+int berr(plbm_batch *b, int code, const std::string &m)
+{
+    if (b) b->err = m;
+    g_batch_err = m;
+    return code;
+}
+}  // namespace
+
+extern "C" {
+
+int plbm_batch_create(unsigned n, const plbm_batch_domain *doms, int precision, plbm_batch **out)
+{
+    if (!doms || !out || n == 0) return berr(nullptr, PLBM_ERR_ARGUMENT, "plbm_batch_create: no domains");
+    if (precision != PLBM_F32 && precision != PLBM_F16S && precision != PLBM_BF16S && precision != PLBM_F64_Q60)
+        return berr(nullptr, PLBM_ERR_ARGUMENT, "batches support PLBM_F32, PLBM_F16S, PLBM_BF16S and PLBM_F64_Q60");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return berr(nullptr, PLBM_ERR_NO_DEVICE, "no CUDA device");
+    auto *b = new plbm_batch();
+    b->prec = precision;
+    if (cudaMalloc(&b->status_pending, sizeof(int)) != cudaSuccess) {
+        delete b;
+        return berr(nullptr, PLBM_ERR_CUDA, "cudaMalloc status");
+    }
+    b->status_d = b->status_pending;
+    auto fail = [&](cudaError_t e, const char *what) {
+        const int rc = berr(b, PLBM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+        delete b;
+        return rc;
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(e, "stream");
+    const bool shifted = precision != PLBM_F64_Q60;
+    const size_t eb = precision == PLBM_F32 ? 4 : precision == PLBM_F64_Q60 ? 8 : 2;
+    std::vector<int8_t> flags_host;
+    for (unsigned i = 0; i < n; ++i) {
+        const plbm_batch_domain &s = doms[i];
+        if (s.inner_w < 2 || s.inner_h < 3 || !(s.relaxation_time > 0.5) || !s.mask) {
+            delete b;
+            return berr(nullptr, PLBM_ERR_ARGUMENT, "domain " + std::to_string(i) + ": need W >= 2, H >= 3, tau > 0.5, a mask");
+        }
+        StepParams d;
+        std::memset(&d, 0, sizeof d);
+        d.W = (int)s.inner_w; d.H = (int)s.inner_h; d.P = (d.W + 31) / 32 * 32;
+        d.N = (unsigned long long)d.P * d.H;
+        b->nodes += (unsigned long long)d.W * d.H;
+        mb(0, 0, 1, d.weight);
+        mb(0, 0, s.inlet_density, d.feq_in);
+        mb(0, 0, s.outlet_density, d.feq_out);
+        d.omega = 1 / s.relaxation_time;
+        d.rho_out = s.outlet_density;
+        d.omegaf = (float)d.omega;
+        d.rho_outf = (float)(shifted ? d.rho_out - 1.0 : d.rho_out);
+        for (int k = 0; k < 9; ++k) {
+            d.weightf[k] = shifted ? 0.0f : (float)d.weight[k];
+            d.feq_inf[k] = (float)(shifted ? d.feq_in[k] - d.weight[k] : d.feq_in[k]);
+            d.feq_outf[k] = (float)(shifted ? d.feq_out[k] - d.weight[k] : d.feq_out[k]);
+            d.q_weight[k] = q60(d.weight[k]); d.q_feq_in[k] = q60(d.feq_in[k]); d.q_feq_out[k] = q60(d.feq_out[k]);
+        }
+        const long double om = d.omega;
+        d.q_om1 = q64(om / 2);
+        d.q_ow49 = q64(om * (4.0 / 9)); d.q_ow9 = q64(om * (1.0 / 9)); d.q_ow36 = q64(om * (1.0 / 36));
+        d.q_k9 = q64(4.5L * om / 9); d.q_k36 = q64(4.5L * om / 36); d.q_o9 = q64(3.0L * om / 9); d.q_o36 = q64(3.0L * om / 36);
+        d.q_rho_out = q60(d.rho_out); d.q_sixth = q64(1.0L / 6); d.q_two_thirds = q64(2.0L / 3);
+        // device buffers of the domain
+        int8_t *flags = nullptr;
+        void *ptrs[8] = {};
+        size_t sizes[8] = { 9 * d.N * eb, 9 * d.N * eb, d.N * 2, (size_t)d.W * d.H, 4 * (size_t)d.W * d.H * 8,
+                            2 * (size_t)d.H * 8, 0, 0 };
+        for (int k = 0; k < 6; ++k) {
+            e = cudaMalloc(&ptrs[k], sizes[k]);
+            if (e != cudaSuccess) return fail(e, "cudaMalloc domain");
+            b->allocs.push_back(ptrs[k]);
+        }
+        d.links = (const uint16_t *)ptrs[2];
+        flags = (int8_t *)ptrs[3];
+        double *res = (double *)ptrs[4];
+        d.rho = res; d.jx = res + (size_t)d.W * d.H; d.jy = res + 2 * (size_t)d.W * d.H; d.jabs = res + 3 * (size_t)d.W * d.H;
+        double *jyc = (double *)ptrs[5];
+        d.nan_protection = 1;
+        d.status = b->status_pending;
+        e = cudaMemcpyAsync(flags, s.mask, (size_t)d.W * d.H, cudaMemcpyHostToDevice, b->stream);
+        if (e == cudaSuccess) e = plbm::launch_links(flags, (uint16_t *)ptrs[2], d.W, d.H, d.P, b->stream);
+        double rest[9];
+        for (int k = 0; k < 9; ++k) rest[k] = shifted ? 0.0 : d.weight[k];
+        if (e == cudaSuccess) e = plbm::launch_fill_lattice(ptrs[0], precision, plbm::STREAM, d.N, rest, b->stream);
+        if (e == cudaSuccess) e = plbm::launch_fill_lattice(ptrs[1], precision, plbm::STREAM, d.N, rest, b->stream);
+        if (e == cudaSuccess) e = plbm::launch_fill_results(d.rho, d.jx, d.jy, d.jabs, (unsigned long long)d.W * d.H, b->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(jyc, 0, 2 * (size_t)d.H * 8, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);   // the mask buffer is the caller's
+        if (e != cudaSuccess) return fail(e, "domain set-up");
+        for (unsigned par = 0; par < 2; ++par) {
+            StepParams q = d;
+            q.lat0 = ptrs[par];
+            q.lat1 = ptrs[par ^ 1u];
+            q.jy_prev = jyc + (size_t)par * d.H;
+            q.jy_next = jyc + (size_t)(par ^ 1u) * d.H;
+            b->host.push_back(q);
+        }
+    }
+    e = cudaMalloc(&b->dom_d, b->host.size() * sizeof(StepParams));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->dom_d, b->host.data(), b->host.size() * sizeof(StepParams), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaMalloc(&b->ticket_d, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->status_d, 0, sizeof(int), b->stream);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    b->blocks = sms * 8;
+    if (e == cudaSuccess) e = b->build_tiles();
+    if (e != cudaSuccess) return fail(e, "batch set-up");
+    *out = b;
+    return PLBM_OK;
+}
+
+void plbm_batch_destroy(plbm_batch *b) { delete b; }
+
+int plbm_batch_set_tile(plbm_batch *b, int tile_w, int tile_h, int blocks_per_sm)
+{
+    if (tile_w < 1 || tile_h < 1 || tile_w * tile_h > 1024 || blocks_per_sm < 1)
+        return berr(b, PLBM_ERR_ARGUMENT, "tile must have 1..1024 threads");
+    b->tile_w = tile_w;
+    b->tile_h = tile_h;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    b->blocks = sms * blocks_per_sm;
+    const cudaError_t e = b->build_tiles();
+    return e == cudaSuccess ? PLBM_OK : berr(b, PLBM_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int plbm_batch_run(plbm_batch *b, unsigned steps, int mode, double *ms_per_step)
+{
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaError_t e = cudaEventRecord(e0, b->stream);
+    const unsigned per_graph = 16;
+    unsigned k = 0;
+    if (mode == PLBM_BATCH_PERSISTENT_GRAPH && steps >= per_graph) {
+        if ((b->t & 1u) && e == cudaSuccess) { e = b->launch(b->t, 0); ++k; }
+        if (e == cudaSuccess) e = b->ensure_graph(per_graph);
+        while (e == cudaSuccess && k + per_graph <= steps - 1) {
+            e = cudaGraphLaunch(b->gexec, b->stream);
+            k += per_graph;
+        }
+    }
+    for (; k < steps && e == cudaSuccess; ++k) {
+        const int last = k + 1 == steps;
+        e = mode == PLBM_BATCH_PER_DOMAIN ? b->launch_per_domain(b->t + k, last) : b->launch(b->t + k, last);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0;
+    if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return berr(b, PLBM_ERR_CUDA, cudaGetErrorString(e));
+    b->t += steps;
+    if (ms_per_step) *ms_per_step = steps ? ms / steps : 0.0;
+    int st = 0;
+    cudaMemcpy(&st, b->status_d, sizeof(int), cudaMemcpyDeviceToHost);
+    if (st) return berr(b, PLBM_ERR_NUMERIC, "a population left the f64_q60 range");
+    return PLBM_OK;
+}
+
+int plbm_batch_autotune(plbm_batch *b, unsigned steps, int *tile_w, int *tile_h, int *blocks_per_sm)
+{
+    static const int cand[][2] = { { 32, 2 }, { 32, 4 }, { 32, 8 }, { 64, 2 }, { 64, 4 }, { 128, 2 }, { 32, 16 } };
+    static const int bps[] = { 4, 8, 16 };
+    double best = 1e300;
+    int bw = b->tile_w, bh = b->tile_h, bb = 8;
+    for (const auto &c : cand)
+        for (int k : bps) {
+            if (plbm_batch_set_tile(b, c[0], c[1], k) != PLBM_OK) continue;
+            double ms = 0;
+            if (plbm_batch_run(b, steps, PLBM_BATCH_PERSISTENT, &ms) != PLBM_OK) return PLBM_ERR_CUDA;
+            if (ms < best) { best = ms; bw = c[0]; bh = c[1]; bb = k; }
+        }
+    const int rc = plbm_batch_set_tile(b, bw, bh, bb);
+    if (tile_w) *tile_w = bw;
+    if (tile_h) *tile_h = bh;
+    if (blocks_per_sm) *blocks_per_sm = bb;
+    return rc;
+}
+
+int plbm_batch_results(plbm_batch *b, unsigned domain, int which, double *out)
+{
+    if (domain >= b->n_domains() || which < 0 || which > 3) return berr(b, PLBM_ERR_ARGUMENT, "bad domain/which");
+    const StepParams &d = b->host[2 * domain];
+    const double *src = which == 0 ? d.rho : which == 1 ? d.jx : which == 2 ? d.jy : d.jabs;
+    const cudaError_t e = cudaMemcpy(out, src, (size_t)d.W * d.H * 8, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? PLBM_OK : berr(b, PLBM_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int plbm_batch_info(plbm_batch *b, unsigned long long *nodes, unsigned *tiles)
+{
+    if (nodes) *nodes = b->nodes;
+    if (tiles) *tiles = b->n_tiles;
+    return PLBM_OK;
+}
+
+const char *plbm_batch_last_error(void) { return g_batch_err.c_str(); }
+
+}  // extern "C"

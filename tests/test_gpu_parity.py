@@ -133,3 +133,52 @@ def test_residual_decreases_and_steady_state_is_reached(plbm):
     assert r < 1e-6 and steps < 200000
     jx = hd.get_x_velocities()
     assert np.all(np.isfinite(jx)) and jx[mask.reshape(-1) == 0].mean() > 0
+
+
+def _batch_domains(plbm, n=5, seed=11):
+    rng = np.random.default_rng(seed)
+    doms = []
+    for i in range(n):
+        w, h = int(rng.integers(40, 140)), int(rng.integers(24, 90))
+        doms.append({"mask": plbm.porous_disks(w, h, seed + i, float(rng.uniform(0.6, 0.8))),
+                     "relaxation_time": float(rng.uniform(0.55, 1.0)),
+                     "inlet_density": float(rng.uniform(1.001, 1.05)), "outlet_density": 1.0})
+    return doms
+
+
+@pytest.mark.parametrize("precision", ["f32", "f16s", "f64_q60"])
+@pytest.mark.parametrize("mode", ["persistent", "persistent_graph", "per_domain"])
+def test_batch_equals_independent_handlers(plbm, precision, mode):
+    """Every domain of a batch ends bit-identical to the same channel run alone by a handler."""
+    doms = _batch_domains(plbm)
+    b = plbm.Batch(doms, precision=precision)
+    b.set_tile(32, 4, 8)
+    steps = 150
+    b.run(steps, mode=mode)
+    for i, d in enumerate(doms):
+        h, w = d["mask"].shape
+        props = plbm.Properties("nptl", "stream", False, 64, steps, steps, "Hagen-Poiseuille", h, w, 0.0, 0.0,
+                                d["inlet_density"], 0.0, 0.0, 1.0, d["relaxation_time"])
+        hd = plbm.create_handler(props, precision=precision, mask=d["mask"])
+        hd.start()
+        hd.block_until_finished()
+        for k, get in enumerate((hd.get_densities, hd.get_x_velocities, hd.get_y_velocities)):
+            assert np.array_equal(b.result(i, k), get()), (i, k)
+        hd.close()
+    b.close()
+
+
+def test_batch_autotune_keeps_results(plbm):
+    """Autotuning times real steps (7 tile shapes x 3 occupancies x 2 steps = 42) and results do not
+    depend on the tile shape it picks."""
+    doms = _batch_domains(plbm, n=3, seed=5)
+    a = plbm.Batch(doms, precision="f32")
+    a.autotune(steps=2)
+    a.run(58)
+    ref = plbm.Batch(doms, precision="f32")
+    ref.run(100, mode="per_domain")
+    for i in range(len(doms)):
+        for k in range(3):
+            assert np.array_equal(a.result(i, k), ref.result(i, k))
+    na, _ = a.info()
+    assert na == sum(d["mask"].size for d in doms)
