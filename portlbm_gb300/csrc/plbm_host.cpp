@@ -574,13 +574,15 @@ struct plbm_handler {
         // Ghost constants and rest state in the arithmetic of the chosen form.
         plbm::StepParams &b = base;
         std::memset(&b, 0, sizeof b);
-        if (prec == PLBM_F64_STRICT || prec == PLBM_F64_FAST || prec == PLBM_F64_Q60) {
+        if (prec != PLBM_F32_REF) {
+            // double constants; the FP32/FP16/BF16 forms round (feq - w) once, from double
             maxwell_boltzmann<double>(0, 0, 1, b.weight);
             maxwell_boltzmann<double>(props.ivx, props.ivy, props.irho, b.feq_in);
             maxwell_boltzmann<double>(props.ovx, props.ovy, props.orho, b.feq_out);
             b.omega = 1 / props.tau;
             b.rho_out = props.orho;
         } else {
+            // the reference's USE_FLOAT build: real_type float throughout
             float w[9], fi[9], fo[9];
             maxwell_boltzmann<float>(0, 0, 1, w);
             maxwell_boltzmann<float>((float)props.ivx, (float)props.ivy, (float)props.irho, fi);
