@@ -7,6 +7,7 @@
 // There is no counterpart in the reference, which runs one domain per handler; this is the
 // "batching" addition of the GB300 build.
 #include "../../include/plbm_c.h"
+#include "plbm_consts.h"
 #include "plbm_kernels.cuh"
 #include "plbm_launch.h"
 
@@ -95,22 +96,6 @@ __global__ void k_batch_single(BatchArgs a, unsigned domain)
 namespace {
 
 using plbm::StepParams;
-
-long long q60(long double x) { return (long long)std::llroundl(x * 1152921504606846976.0L); }
-long long q64(long double c)
-{
-    const long double v = c * 18446744073709551616.0L + 0.5L;
-    return (long long)(v >= 18446744073709551615.0L ? 18446744073709551615ull : (unsigned long long)v);
-}
-
-void mb(double ux, double uy, double rho, double *t)
-{
-    static const double w[9] = { 1.0 / 36, 1.0 / 9, 1.0 / 36, 1.0 / 9, 4.0 / 9, 1.0 / 9, 1.0 / 36, 1.0 / 9, 1.0 / 36 };
-    for (int d = 0; d < 9; ++d) {
-        const int vx = (d % 3) - 1, vy = (d / 3) - 1;
-        t[d] = w[d] * (rho + 3 * (vx * ux + vy * uy) + 9.0 / 2 * std::pow(vx * ux + vy * uy, 2) - 3.0 / 2 * (ux * ux + uy * uy));
-    }
-}
 
 }  // namespace
 
@@ -274,9 +259,9 @@ int plbm_batch_create(unsigned n, const plbm_batch_domain *doms, int precision, 
         d.W = (int)s.inner_w; d.H = (int)s.inner_h; d.P = (d.W + 31) / 32 * 32;
         d.N = (unsigned long long)d.P * d.H;
         b->nodes += (unsigned long long)d.W * d.H;
-        mb(0, 0, 1, d.weight);
-        mb(0, 0, s.inlet_density, d.feq_in);
-        mb(0, 0, s.outlet_density, d.feq_out);
+        plbm::maxwell_boltzmann<double>(0, 0, 1, d.weight);
+        plbm::maxwell_boltzmann<double>(0, 0, s.inlet_density, d.feq_in);
+        plbm::maxwell_boltzmann<double>(0, 0, s.outlet_density, d.feq_out);
         d.omega = 1 / s.relaxation_time;
         d.rho_out = s.outlet_density;
         d.omegaf = (float)d.omega;
@@ -285,13 +270,8 @@ int plbm_batch_create(unsigned n, const plbm_batch_domain *doms, int precision, 
             d.weightf[k] = shifted ? 0.0f : (float)d.weight[k];
             d.feq_inf[k] = (float)(shifted ? d.feq_in[k] - d.weight[k] : d.feq_in[k]);
             d.feq_outf[k] = (float)(shifted ? d.feq_out[k] - d.weight[k] : d.feq_out[k]);
-            d.q_weight[k] = q60(d.weight[k]); d.q_feq_in[k] = q60(d.feq_in[k]); d.q_feq_out[k] = q60(d.feq_out[k]);
         }
-        const long double om = d.omega;
-        d.q_om1 = q64(om / 2);
-        d.q_ow49 = q64(om * (4.0 / 9)); d.q_ow9 = q64(om * (1.0 / 9)); d.q_ow36 = q64(om * (1.0 / 36));
-        d.q_k9 = q64(4.5L * om / 9); d.q_k36 = q64(4.5L * om / 36); d.q_o9 = q64(3.0L * om / 9); d.q_o36 = q64(3.0L * om / 36);
-        d.q_rho_out = q60(d.rho_out); d.q_sixth = q64(1.0L / 6); d.q_two_thirds = q64(2.0L / 3);
+        plbm::fill_q60_constants(d);
         // device buffers of the domain
         int8_t *flags = nullptr;
         void *ptrs[8] = {};

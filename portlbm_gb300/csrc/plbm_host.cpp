@@ -12,6 +12,7 @@
 // (every other step's values are overwritten before any copy in the reference); runs of steps
 // between copies are replayed from a captured CUDA graph.
 #include "../../include/plbm_c.h"
+#include "plbm_consts.h"
 #include "plbm_json.hpp"
 #include "plbm_launch.h"
 
@@ -366,31 +367,11 @@ std::vector<int8_t> make_flags(const Props &p, const std::vector<int8_t> *mask)
     return f;
 }
 
-// maxwell_boltzmann_distribution (simulation.hpp:333-350), in real_type R.
-template <typename R>
-void maxwell_boltzmann(R ux, R uy, R rho, R *t)
-{
-    static const R W[9] = { (R)(1.0 / 36), (R)(1.0 / 9), (R)(1.0 / 36), (R)(1.0 / 9), (R)(4.0 / 9),
-                            (R)(1.0 / 9), (R)(1.0 / 36), (R)(1.0 / 9), (R)(1.0 / 36) };
-    for (int d = 0; d < 9; ++d) {
-        const int vx = (d % 3) - 1, vy = (d / 3) - 1;
-        t[d] = (R)(W[d] * (rho + 3 * (vx * ux + vy * uy) + 9.0 / 2 * std::pow((double)(vx * ux + vy * uy), 2) -
-                           3.0 / 2 * (ux * ux + uy * uy)));
-    }
-}
-
 int alg_index(const std::string &a) { return a == "nptl" ? 0 : a == "lptl" ? 1 : a == "npol" ? 2 : 3; }
 int layout_index(const std::string &l) { return l == "collision" ? 0 : l == "stream" ? 1 : 2; }
 size_t storage_bytes(int prec) { return (prec <= 1 || prec == PLBM_F64_Q60) ? 8 : prec <= 3 ? 4 : 2; }
 
-// round(x * 2^60) (populations) and round(c * 2^64) for constants 0 <= c < 1, in long double.
-long long q60(long double x) { return (long long)std::llroundl(x * 1152921504606846976.0L); }
-long long q64(long double c)
-{
-    const long double v = c * 18446744073709551616.0L + 0.5L;
-    const unsigned long long u = v >= 18446744073709551615.0L ? 18446744073709551615ull : (unsigned long long)v;
-    return (long long)u;   // bit pattern of the unsigned Q0.64 value
-}
+using plbm::maxwell_boltzmann;
 
 thread_local std::string g_tls_error;
 std::mutex g_create_mu;
@@ -602,20 +583,7 @@ struct plbm_handler {
         // outlet: f1+f4+f7+2(f8+f5+f2) carries exactly 1 in rest weights, so xv = (1 - rho_out) + sum(df)
         b.rho_outf = shifted ? (float)(b.rho_out - 1.0) : (float)b.rho_out;
         {
-            // Q60 constants from the reference's double constants (1/tau, w_d, 1.0/6, 2.0/3)
-            const long double om = (long double)b.omega, w9 = 1.0 / 9, w36 = 1.0 / 36, w49 = 4.0 / 9;
-            b.q_om1 = q64(om / 2);   // the Q60 kernel applies omega as twice omega/2
-            b.q_ow49 = q64(om * w49); b.q_ow9 = q64(om * w9); b.q_ow36 = q64(om * w36);
-            b.q_k9 = q64(4.5L * om * w9); b.q_k36 = q64(4.5L * om * w36);
-            b.q_o9 = q64(3.0L * om * w9); b.q_o36 = q64(3.0L * om * w36);
-            b.q_rho_out = q60((long double)b.rho_out);
-            b.q_sixth = q64((long double)(1.0 / 6));
-            b.q_two_thirds = q64((long double)(2.0 / 3));
-            for (int d = 0; d < 9; ++d) {
-                b.q_weight[d] = q60((long double)b.weight[d]);
-                b.q_feq_in[d] = q60((long double)b.feq_in[d]);
-                b.q_feq_out[d] = q60((long double)b.feq_out[d]);
-            }
+            plbm::fill_q60_constants(b);
             b.status = status_d;
             if (prec == PLBM_F64_Q60) {
                 if (!(props.tau > 0.5))
