@@ -236,6 +236,44 @@ def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, 
     return study
 
 
+def batch_domains(plbm, n=256, seed=2024):
+    """256 independent porous channels: W, H uniform in 64..1024, disks r in [3, 12] at porosity
+    uniform in [0.6, 0.8], tau uniform in [0.55, 1.0], inlet density uniform in [1.001, 1.05]."""
+    rng = np.random.default_rng(seed)
+    doms = []
+    for i in range(n):
+        w, h = int(rng.integers(64, 1025)), int(rng.integers(64, 1025))
+        doms.append({"mask": plbm.porous_disks(w, h, seed * 1000 + i, float(rng.uniform(0.6, 0.8))),
+                     "relaxation_time": float(rng.uniform(0.55, 1.0)),
+                     "inlet_density": float(rng.uniform(1.001, 1.05)), "outlet_density": 1.0})
+    return doms
+
+
+def batch_study(plbm, steps=100, precisions=("f32", "f16s")):
+    """Aggregate MLUPS of 256 uneven domains: one persistent tile-queue launch per step replayed from a
+    CUDA graph (tiles autotuned) against one launch per domain per step."""
+    doms = batch_domains(plbm)
+    out = {"domains": len(doms)}
+    for prec in precisions:
+        b = plbm.Batch(doms, precision=prec)
+        nodes, _ = b.info()
+        tile = b.autotune(steps=3)
+        _, tiles = b.info()
+        b.run(16, mode="persistent_graph")
+        ms_graph = b.run(steps, mode="persistent_graph")
+        ms_pers = b.run(steps, mode="persistent")
+        b.run(4, mode="per_domain")
+        ms_per = b.run(steps, mode="per_domain")
+        bpn = BYTES_PER_NODE[prec]
+        out[prec] = {"nodes": nodes, "tiles": tiles, "tile": list(tile),
+                     "mlups_persistent_graph": round(nodes / ms_graph / 1e3, 1),
+                     "mlups_persistent": round(nodes / ms_pers / 1e3, 1),
+                     "mlups_per_domain_launches": round(nodes / ms_per / 1e3, 1),
+                     "hbm_gbs_persistent_graph": round(bpn * nodes / ms_graph / 1e6, 1)}
+        b.close()
+    return out
+
+
 def load_traffic(kind: str, nodes: int):
     v = TRAFFIC_PER_NODE.get(kind)
     return None if v is None else round(v * nodes)
@@ -371,6 +409,7 @@ def main():
 
     err = err_vs_oracle(plbm, args.precision) if rank == 0 else None
     study = precision_study(plbm) if (rank == 0 and not args.no_study and not args.no_variants) else None
+    batch = batch_study(plbm) if (rank == 0 and not args.no_study and not args.no_variants) else None
 
     # -- CPU baseline (rank 0, N = 1) --
     cpu = None
@@ -405,6 +444,7 @@ def main():
             "cpu_baseline": cpu,
             "variants": variants,
             "precision_study": study,
+            "batch_study": batch,
         }
         print(json.dumps(line), flush=True)
 
