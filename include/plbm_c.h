@@ -225,7 +225,9 @@ enum { PLBM_BATCH_PERSISTENT = 0, PLBM_BATCH_PERSISTENT_GRAPH = 1, PLBM_BATCH_PE
 
 int plbm_batch_create(unsigned n, const plbm_batch_domain *domains, int precision, plbm_batch **out);
 void plbm_batch_destroy(plbm_batch *b);
-/* Tile shape (threads of one block) and resident blocks per SM of the persistent launch. */
+/* Tile shape and resident blocks per SM of the persistent launch: a block of tile_w x (tile_h & 255)
+ * threads, each sweeping (tile_h >> 8) rows (at least 1), so a tile covers
+ * tile_w x ((tile_h & 255) * rows) nodes. */
 int plbm_batch_set_tile(plbm_batch *b, int tile_w, int tile_h, int blocks_per_sm);
 /* Times `steps` persistent steps for each candidate tile shape and occupancy, keeps the fastest
  * (the timed steps advance the batch). */

@@ -27,7 +27,7 @@ struct BatchArgs {
     const int *tiles_x;            // tiles per row of each domain
     unsigned n_tiles;
     unsigned *ticket;              // work-queue counter, zeroed before every step
-    int tile_w, tile_h;
+    int tile_w, tile_h, tile_rows;   // a tile is tile_w x (tile_h * tile_rows) nodes
     unsigned parity;
     int write_results;
 };
@@ -66,10 +66,14 @@ __global__ void k_batch(BatchArgs a)
         }
         __syncthreads();
         const int local = (int)a.tile_local[t], txs = a.tiles_x[dom];
-        const int xi = (local % txs) * a.tile_w + threadIdx.x, yi = (local / txs) * a.tile_h + threadIdx.y;
-        if (xi < sp.W && yi < sp.H) {
-            const int xs[1] = { xi }, ys[1] = { yi };
-            update_two_lattice_rows<PREC, STREAM, 1>(xs, ys, sp);
+        const int xi = (local % txs) * a.tile_w + threadIdx.x;
+        const int y0 = (local / txs) * a.tile_h * a.tile_rows + threadIdx.y;
+        for (int r = 0; r < a.tile_rows; ++r) {
+            const int yi = y0 + r * a.tile_h;
+            if (xi < sp.W && yi < sp.H) {
+                const int xs[1] = { xi }, ys[1] = { yi };
+                update_two_lattice_rows<PREC, STREAM, 1>(xs, ys, sp);
+            }
         }
         __syncthreads();   // s_tile / s_dom are rewritten for the next tile
     }
@@ -108,7 +112,7 @@ struct plbm_batch {
     int *tiles_x_d = nullptr;
     int *status_d = nullptr, *status_pending = nullptr;
     unsigned n_tiles = 0, t = 0;
-    int tile_w = 32, tile_h = 4, blocks = 0;
+    int tile_w = 32, tile_h = 4, tile_rows = 8, blocks = 0;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t gexec = nullptr;
     unsigned graph_steps = 0;
@@ -138,7 +142,7 @@ struct plbm_batch {
         std::vector<int> tx;
         for (unsigned i = 0; i < n_domains(); ++i) {
             const StepParams &d = host[2 * i];
-            const int nx = (d.W + tile_w - 1) / tile_w, ny = (d.H + tile_h - 1) / tile_h;
+            const int nx = (d.W + tile_w - 1) / tile_w, ny = (d.H + tile_h * tile_rows - 1) / (tile_h * tile_rows);
             tx.push_back(nx);
             for (int k = 0; k < nx * ny; ++k) { dom.push_back(i); loc.push_back((unsigned)k); }
         }
@@ -159,7 +163,7 @@ struct plbm_batch {
     plbm::BatchArgs args(unsigned parity, int write_results) const
     {
         return plbm::BatchArgs{ dom_d, tile_domain_d, tile_local_d, tiles_x_d, n_tiles, ticket_d,
-                                tile_w, tile_h, parity, write_results };
+                                tile_w, tile_h, tile_rows, parity, write_results };
     }
 
     cudaError_t launch(unsigned step, int write_results)
@@ -329,7 +333,10 @@ int plbm_batch_set_tile(plbm_batch *b, int tile_w, int tile_h, int blocks_per_sm
     if (tile_w < 1 || tile_h < 1 || tile_w * tile_h > 1024 || blocks_per_sm < 1)
         return berr(b, PLBM_ERR_ARGUMENT, "tile must have 1..1024 threads");
     b->tile_w = tile_w;
-    b->tile_h = tile_h;
+    // tile_h carries the rows each thread sweeps in its upper bits: tile_h = threads_y + 256 * rows
+    b->tile_h = tile_h & 255;
+    b->tile_rows = std::max(1, tile_h >> 8);
+    if (b->tile_w * b->tile_h > 1024) return berr(b, PLBM_ERR_ARGUMENT, "tile must have 1..1024 threads");
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     b->blocks = sms * blocks_per_sm;
@@ -374,7 +381,9 @@ int plbm_batch_run(plbm_batch *b, unsigned steps, int mode, double *ms_per_step)
 
 int plbm_batch_autotune(plbm_batch *b, unsigned steps, int *tile_w, int *tile_h, int *blocks_per_sm)
 {
-    static const int cand[][2] = { { 32, 2 }, { 32, 4 }, { 32, 8 }, { 64, 2 }, { 64, 4 }, { 128, 2 }, { 32, 16 } };
+    // threads_x, threads_y + 256 * rows swept per thread
+    static const int cand[][2] = { { 32, 4 + 256 * 1 }, { 32, 4 + 256 * 4 }, { 32, 4 + 256 * 8 }, { 32, 8 + 256 * 4 },
+                                   { 64, 2 + 256 * 8 }, { 64, 4 + 256 * 4 }, { 128, 2 + 256 * 4 } };
     static const int bps[] = { 4, 8, 16 };
     double best = 1e300;
     int bw = b->tile_w, bh = b->tile_h, bb = 8;
@@ -387,7 +396,7 @@ int plbm_batch_autotune(plbm_batch *b, unsigned steps, int *tile_w, int *tile_h,
         }
     const int rc = plbm_batch_set_tile(b, bw, bh, bb);
     if (tile_w) *tile_w = bw;
-    if (tile_h) *tile_h = bh;
+    if (tile_h) *tile_h = bh;   // threads_y + 256 * rows
     if (blocks_per_sm) *blocks_per_sm = bb;
     return rc;
 }

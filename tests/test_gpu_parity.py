@@ -170,7 +170,7 @@ def test_batch_equals_independent_handlers(plbm, precision, mode):
 
 def test_batch_autotune_keeps_results(plbm):
     """Autotuning times real steps (7 tile shapes x 3 occupancies x 2 steps = 42) and results do not
-    depend on the tile shape it picks."""
+    depend on the tile shape (threads, rows per thread) it picks."""
     doms = _batch_domains(plbm, n=3, seed=5)
     a = plbm.Batch(doms, precision="f32")
     a.autotune(steps=2)
