@@ -330,13 +330,13 @@ void plbm_batch_destroy(plbm_batch *b) { delete b; }
 
 int plbm_batch_set_tile(plbm_batch *b, int tile_w, int tile_h, int blocks_per_sm)
 {
-    if (tile_w < 1 || tile_h < 1 || tile_w * tile_h > 1024 || blocks_per_sm < 1)
+    // tile_h carries the rows each thread sweeps in its upper bits: tile_h = threads_y + 256 * rows
+    const int ty = tile_h & 255, rows = std::max(1, tile_h >> 8);
+    if (tile_w < 1 || ty < 1 || tile_w * ty > 1024 || blocks_per_sm < 1)
         return berr(b, PLBM_ERR_ARGUMENT, "tile must have 1..1024 threads");
     b->tile_w = tile_w;
-    // tile_h carries the rows each thread sweeps in its upper bits: tile_h = threads_y + 256 * rows
-    b->tile_h = tile_h & 255;
-    b->tile_rows = std::max(1, tile_h >> 8);
-    if (b->tile_w * b->tile_h > 1024) return berr(b, PLBM_ERR_ARGUMENT, "tile must have 1..1024 threads");
+    b->tile_h = ty;
+    b->tile_rows = rows;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     b->blocks = sms * blocks_per_sm;
@@ -386,7 +386,7 @@ int plbm_batch_autotune(plbm_batch *b, unsigned steps, int *tile_w, int *tile_h,
                                    { 64, 2 + 256 * 8 }, { 64, 4 + 256 * 4 }, { 128, 2 + 256 * 4 } };
     static const int bps[] = { 4, 8, 16 };
     double best = 1e300;
-    int bw = b->tile_w, bh = b->tile_h, bb = 8;
+    int bw = b->tile_w, bh = b->tile_h + 256 * b->tile_rows, bb = 8;
     for (const auto &c : cand)
         for (int k : bps) {
             if (plbm_batch_set_tile(b, c[0], c[1], k) != PLBM_OK) continue;
