@@ -238,6 +238,32 @@ int plbm_batch_results(plbm_batch *b, unsigned domain, int which, double *out);
 int plbm_batch_info(plbm_batch *b, unsigned long long *nodes, unsigned *tiles);
 const char *plbm_batch_last_error(void);
 
+/* ---- learned warm start (no counterpart in the reference) -----------------------------------
+ * plbm_set_equilibrium: replaces the state of an nptl/lptl handler that has not stepped (or has
+ * stepped an even number of times) by the equilibrium populations of the given inner fields
+ * rho, jx, jy (W*H host doubles each; solid entries ignored).
+ * plbm_nn_*: the convolutional neural operator's kernels.  Activations NHWC bfloat16 on the
+ * device; weights W[co][(ky*3+kx)*Cin+ci] bfloat16; 3x3 convolutions with zero padding run as
+ * implicit GEMMs on the BF16 tensor cores with FP32 accumulation; gw/gb accumulate (FP32). */
+int plbm_set_equilibrium(plbm_handler *h, const double *rho, const double *jx, const double *jy);
+int plbm_nn_conv_fwd(const void *x, const void *w, const float *bias, void *y, int N, int H, int W, int Cin, int Cout,
+                     int relu, void *stream);
+int plbm_nn_conv_dgrad(const void *g, const void *w, void *gx, int N, int H, int W, int Cin, int Cout, void *stream);
+int plbm_nn_conv_wgrad(const void *x, const void *g, float *gw, float *gb, int N, int H, int W, int Cin, int Cout,
+                       void *stream);
+int plbm_nn_relu_bwd(const void *y, void *g, long long n, void *stream);
+int plbm_nn_pool2(const void *x, void *y, int N, int H, int W, int C, void *stream);
+int plbm_nn_pool2_bwd(const void *gy, void *gx, int N, int H, int W, int C, void *stream);
+int plbm_nn_up2(const void *x, void *y, int N, int H, int W, int C, void *stream);
+int plbm_nn_up2_bwd(const void *gy, void *gx, int N, int H, int W, int C, void *stream);
+int plbm_nn_add(const void *a, const void *b, void *y, long long n, void *stream);
+int plbm_nn_mse(const void *pred, const float *target, const int8_t *mask, void *grad, float *loss, long long P, int C,
+                float inv_count, void *stream);
+int plbm_nn_adam(float *w, const float *g, float *m, float *v, void *w_bf16, long long n, float lr, float b1, float b2,
+                 float eps, int t, void *stream);
+int plbm_nn_assemble(const int8_t *mask, const float *inlet_density, const float *outlet_density,
+                     const float *relaxation_time, void *y, int N, int H, int W, int C, void *stream);
+
 /* Last error message for h (or of the last failed create when h is NULL). */
 const char *plbm_last_error(const plbm_handler *h);
 const char *plbm_version(void);

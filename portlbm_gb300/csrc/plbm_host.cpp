@@ -1079,6 +1079,30 @@ int plbm_porous_disks(unsigned inner_w, unsigned inner_h, uint64_t seed, double 
     return rc == PLBM_OK ? count : rc;
 }
 
+int plbm_set_equilibrium(plbm_handler *h, const double *rho, const double *jx, const double *jy)
+{
+    return guarded(h, [&] {
+        if (h->alg != 0 && h->alg != 1) fail(PLBM_ERR_ARGUMENT, "plbm_set_equilibrium supports nptl and lptl");
+        if (h->worker.joinable()) fail(PLBM_ERR_ARGUMENT, "plbm_set_equilibrium while the step loop runs");
+        const unsigned par = h->iteration.load() & 1u;
+        double *tmp = nullptr;
+        cuda_check(cudaMalloc(&tmp, 3 * h->nres * sizeof(double)), "cudaMalloc fields");
+        std::unique_ptr<double, decltype(&cudaFree)> keep(tmp, &cudaFree);
+        const double *src[3] = { rho, jx, jy };
+        for (int i = 0; i < 3; ++i)
+            cuda_check(cudaMemcpyAsync(tmp + i * h->nres, src[i], h->nres * sizeof(double), cudaMemcpyHostToDevice,
+                                       h->stream), "H2D fields");
+        cuda_check(plbm::launch_set_equilibrium(h->lat[par], h->prec, h->lay, h->base, tmp, tmp + h->nres,
+                                                tmp + 2 * h->nres, h->stream), "equilibrium");
+        // the outlet reads the previous step's jy of column x' = W-2
+        std::vector<double> col(h->H);
+        for (int y = 0; y < h->H; ++y) col[y] = jy[(size_t)y * h->W + h->W - 2];
+        cuda_check(cudaMemcpyAsync(h->jy_d + (size_t)par * h->H, col.data(), h->H * sizeof(double),
+                                   cudaMemcpyHostToDevice, h->stream), "H2D jy");
+        cuda_check(cudaStreamSynchronize(h->stream), "equilibrium");
+    });
+}
+
 int plbm_sync_results(plbm_handler *h)
 {
     return guarded(h, [&] { h->copy_results(); });

@@ -24,6 +24,9 @@ cudaError_t launch_reduce_results(const double *rho, const double *jx, const dou
 // FP64 sums over fluid nodes: out2 = {sum |j - j_prev|^2, sum |j|^2}; then j_prev = j.
 cudaError_t launch_residual(const double *jx, const double *jy, double *jx_prev, double *jy_prev, const int8_t *flags,
                             unsigned long long n, double *out2_dev, cudaStream_t s);
+// Equilibrium populations of the fields rho, jx, jy (device, W*H doubles) into lattice `lat`.
+cudaError_t launch_set_equilibrium(void *lat, int prec, int lay, const StepParams &p, const double *rho,
+                                   const double *jx, const double *jy, cudaStream_t s);
 int max_threads_for(int alg, int prec, int lay);
 
 }  // namespace plbm

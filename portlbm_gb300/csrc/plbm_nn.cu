@@ -1,0 +1,408 @@
+// plbm_nn.cu — the convolutional neural operator's kernels: 3x3 "same" convolutions as implicit
+// GEMMs on the BF16 tensor cores (mma.sync m16n8k16, FP32 accumulate) for the forward pass, the
+// data gradient and the weight gradient; 2x2 average pooling, nearest upsampling, skip addition,
+// ReLU backward, the masked MSE loss and Adam.  Activations are NHWC bfloat16; weights are
+// W[co][k] with k = (ky * 3 + kx) * Cin + ci (bfloat16, FP32 master copy updated by Adam).
+//
+// No counterpart in the reference: this is the learned warm-start addition of the GB300 build.
+#include "../../include/plbm_c.h"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace {
+
+constexpr int BM = 128, BN = 64, BK = 32, PAD = 8, THREADS = 256;
+
+enum Mode { FWD = 0, DGRAD = 1, WGRAD = 2 };
+
+struct ConvArgs {
+    const __nv_bfloat16 *x;    // FWD/WGRAD: input [N,H,W,Cin]
+    const __nv_bfloat16 *g;    // DGRAD/WGRAD: gradient of the output [N,H,W,Cout]
+    const __nv_bfloat16 *w;    // [Cout][9*Cin]
+    const float *bias;         // FWD: [Cout] or null
+    __nv_bfloat16 *y;          // FWD: output; DGRAD: gradient of the input
+    float *gw;                 // WGRAD: [Cout][9*Cin] accumulated (atomicAdd)
+    int N, H, W, Cin, Cout, relu;
+    int M, Ncols, K;           // GEMM sizes of the mode
+    int k_chunk;               // WGRAD: pixels per block (split K)
+};
+
+__device__ __forceinline__ __nv_bfloat16 bzero() { return __float2bfloat16_rn(0.0f); }
+
+// Element (m, k) of the GEMM's A operand and (n, k) of its B operand for each mode.
+template <int MODE>
+__device__ __forceinline__ __nv_bfloat16 load_a(const ConvArgs &a, int m, int k)
+{
+    if (m >= a.M || k >= a.K) return bzero();
+    if (MODE == FWD || MODE == DGRAD) {
+        const int C = MODE == FWD ? a.Cin : a.Cout;
+        const int tap = k / C, c = k - tap * C, ky = tap / 3, kx = tap - ky * 3;
+        const int x = m % a.W, t = m / a.W, yv = t % a.H, n = t / a.H;
+        const int sy = MODE == FWD ? yv + ky - 1 : yv - ky + 1, sx = MODE == FWD ? x + kx - 1 : x - kx + 1;
+        if (sy < 0 || sy >= a.H || sx < 0 || sx >= a.W) return bzero();
+        const __nv_bfloat16 *src = MODE == FWD ? a.x : a.g;
+        return src[(((size_t)n * a.H + sy) * a.W + sx) * C + c];
+    } else {   // WGRAD: A[co][pixel] = g[pixel][co]
+        return a.g[(size_t)k * a.Cout + m];
+    }
+}
+
+template <int MODE>
+__device__ __forceinline__ __nv_bfloat16 load_b(const ConvArgs &a, int ncol, int k)
+{
+    if (ncol >= a.Ncols || k >= a.K) return bzero();
+    if (MODE == FWD) {
+        return a.w[(size_t)ncol * (9 * a.Cin) + k];
+    } else if (MODE == DGRAD) {   // B[ci][(tap, co)] = W[co][(tap, ci)]
+        const int tap = k / a.Cout, co = k - tap * a.Cout;
+        return a.w[(size_t)co * (9 * a.Cin) + tap * a.Cin + ncol];
+    } else {   // WGRAD: B[(tap, ci)][pixel] = x[pixel + offset(tap)][ci]
+        const int tap = ncol / a.Cin, ci = ncol - tap * a.Cin, ky = tap / 3, kx = tap - ky * 3;
+        const int p = k, x = p % a.W, t = p / a.W, yv = t % a.H, n = t / a.H;
+        const int sy = yv + ky - 1, sx = x + kx - 1;
+        if (sy < 0 || sy >= a.H || sx < 0 || sx >= a.W) return bzero();
+        return a.x[(((size_t)n * a.H + sy) * a.W + sx) * a.Cin + ci];
+    }
+}
+
+__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], const uint32_t b[2])
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// C[BM x BN] tile of block (blockIdx.x over M, blockIdx.y over N); WGRAD splits K over blockIdx.z.
+template <int MODE>
+__global__ void __launch_bounds__(THREADS) k_conv(ConvArgs a)
+{
+    __shared__ __align__(16) __nv_bfloat16 As[BM][BK + PAD];
+    __shared__ __align__(16) __nv_bfloat16 Bs[BN][BK + PAD];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int wm = warp & 3, wn = warp >> 2;          // 4 x 2 warps, 32 x 32 each
+    const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    int k_begin = 0, k_end = a.K;
+    if (MODE == WGRAD) {
+        k_begin = blockIdx.z * a.k_chunk;
+        k_end = min(a.K, k_begin + a.k_chunk);
+    }
+    float acc[2][4][4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.f;
+    const int grp = lane >> 2, tig = lane & 3;
+    for (int k0 = k_begin; k0 < k_end; k0 += BK) {
+        for (int i = tid; i < BM * BK; i += THREADS) {
+            const int r = i / BK, c = i % BK, k = k0 + c;
+            As[r][c] = k < k_end ? load_a<MODE>(a, m0 + r, k) : bzero();
+        }
+        for (int i = tid; i < BN * BK; i += THREADS) {
+            const int r = i / BK, c = i % BK, k = k0 + c;
+            Bs[r][c] = k < k_end ? load_b<MODE>(a, n0 + r, k) : bzero();
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; kk += 16) {
+            uint32_t af[2][4], bf[4][2];
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const int r = wm * 32 + i * 16 + grp;
+                af[i][0] = *reinterpret_cast<const uint32_t *>(&As[r][kk + tig * 2]);
+                af[i][1] = *reinterpret_cast<const uint32_t *>(&As[r + 8][kk + tig * 2]);
+                af[i][2] = *reinterpret_cast<const uint32_t *>(&As[r][kk + tig * 2 + 8]);
+                af[i][3] = *reinterpret_cast<const uint32_t *>(&As[r + 8][kk + tig * 2 + 8]);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int c = wn * 32 + j * 8 + grp;
+                bf[j][0] = *reinterpret_cast<const uint32_t *>(&Bs[c][kk + tig * 2]);
+                bf[j][1] = *reinterpret_cast<const uint32_t *>(&Bs[c][kk + tig * 2 + 8]);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) mma16816(acc[i][j], af[i], bf[j]);
+        }
+        __syncthreads();
+    }
+    // epilogue
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int m = m0 + wm * 32 + i * 16 + grp + (r >= 2 ? 8 : 0);
+                const int n = n0 + wn * 32 + j * 8 + tig * 2 + (r & 1);
+                if (m >= a.M || n >= a.Ncols) continue;
+                float v = acc[i][j][r];
+                if (MODE == FWD) {
+                    if (a.bias) v += a.bias[n];
+                    if (a.relu) v = fmaxf(v, 0.f);
+                    a.y[(size_t)m * a.Cout + n] = __float2bfloat16_rn(v);
+                } else if (MODE == DGRAD) {
+                    a.y[(size_t)m * a.Cin + n] = __float2bfloat16_rn(v);
+                } else {
+                    atomicAdd(&a.gw[(size_t)m * (9 * a.Cin) + n], v);
+                }
+            }
+}
+
+__global__ void k_bias_grad(const __nv_bfloat16 *g, float *gb, long long P, int C)
+{
+    // one block per channel group of 32 channels x 8 pixel rows
+    const int c = blockIdx.y * 32 + (threadIdx.x & 31);
+    if (c >= C) return;
+    float s = 0.f;
+    for (long long p = blockIdx.x * 8 + (threadIdx.x >> 5); p < P; p += (long long)gridDim.x * 8)
+        s += __bfloat162float(g[p * C + c]);
+    atomicAdd(&gb[c], s);
+}
+
+__global__ void k_relu_bwd(const __nv_bfloat16 *y, __nv_bfloat16 *g, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        if (!(__bfloat162float(y[i]) > 0.f)) g[i] = __float2bfloat16_rn(0.f);
+}
+
+__global__ void k_pool2(const __nv_bfloat16 *x, __nv_bfloat16 *y, int N, int H, int W, int C)
+{
+    const int Ho = H / 2, Wo = W / 2;
+    const long long total = (long long)N * Ho * Wo * C;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        long long t = i / C;
+        const int xo = (int)(t % Wo); t /= Wo;
+        const int yo = (int)(t % Ho);
+        const int n = (int)(t / Ho);
+        const size_t b = (((size_t)n * H + 2 * yo) * W + 2 * xo) * C + c;
+        const float s = __bfloat162float(x[b]) + __bfloat162float(x[b + C]) + __bfloat162float(x[b + (size_t)W * C]) +
+                        __bfloat162float(x[b + (size_t)W * C + C]);
+        y[i] = __float2bfloat16_rn(0.25f * s);
+    }
+}
+
+__global__ void k_pool2_bwd(const __nv_bfloat16 *gy, __nv_bfloat16 *gx, int N, int H, int W, int C)
+{
+    const long long total = (long long)N * H * W * C;
+    const int Ho = H / 2, Wo = W / 2;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        long long t = i / C;
+        const int x = (int)(t % W); t /= W;
+        const int yv = (int)(t % H);
+        const int n = (int)(t / H);
+        gx[i] = __float2bfloat16_rn(0.25f * __bfloat162float(gy[(((size_t)n * Ho + yv / 2) * Wo + x / 2) * C + c]));
+    }
+}
+
+__global__ void k_up2(const __nv_bfloat16 *x, __nv_bfloat16 *y, int N, int H, int W, int C)   // H, W: output
+{
+    const long long total = (long long)N * H * W * C;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        long long t = i / C;
+        const int xx = (int)(t % W); t /= W;
+        const int yy = (int)(t % H);
+        const int n = (int)(t / H);
+        y[i] = x[(((size_t)n * (H / 2) + yy / 2) * (W / 2) + xx / 2) * C + c];
+    }
+}
+
+__global__ void k_up2_bwd(const __nv_bfloat16 *gy, __nv_bfloat16 *gx, int N, int H, int W, int C)   // H, W: input
+{
+    const long long total = (long long)N * H * W * C;
+    const int Ho = 2 * H, Wo = 2 * W;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i % C);
+        long long t = i / C;
+        const int x = (int)(t % W); t /= W;
+        const int yv = (int)(t % H);
+        const int n = (int)(t / H);
+        const size_t b = (((size_t)n * Ho + 2 * yv) * Wo + 2 * x) * C + c;
+        gx[i] = __float2bfloat16_rn(__bfloat162float(gy[b]) + __bfloat162float(gy[b + C]) +
+                                    __bfloat162float(gy[b + (size_t)Wo * C]) + __bfloat162float(gy[b + (size_t)Wo * C + C]));
+    }
+}
+
+__global__ void k_add(const __nv_bfloat16 *a, const __nv_bfloat16 *b, __nv_bfloat16 *y, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] = __float2bfloat16_rn(__bfloat162float(a[i]) + __bfloat162float(b[i]));
+}
+
+// Masked mean squared error over fluid pixels of C channels: loss += sum / count, grad = 2 (p - t) / count.
+__global__ void k_mse(const __nv_bfloat16 *pred, const float *target, const int8_t *mask, __nv_bfloat16 *grad,
+                      float *loss, long long P, int C, float inv_count)
+{
+    float s = 0.f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < P * C; i += (long long)gridDim.x * blockDim.x) {
+        const long long p = i / C;
+        float gval = 0.f;
+        if (mask[p] == 0) {
+            const float d = __bfloat162float(pred[i]) - target[i];
+            s += d * d;
+            gval = 2.f * d * inv_count;
+        }
+        grad[i] = __float2bfloat16_rn(gval);
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, s * inv_count);
+}
+
+__global__ void k_adam(float *w, const float *g, float *m, float *v, __nv_bfloat16 *wb, long long n, float lr, float b1,
+                       float b2, float eps, float c1, float c2)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi, vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float wi = w[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+        w[i] = wi;
+        if (wb) wb[i] = __float2bfloat16_rn(wi);
+    }
+}
+
+// Network input: channel 0 fluid(0)/solid(1) mask, then inlet density, outlet density and
+// relaxation time as constant planes (each shifted/scaled to O(1)); channels beyond 4 are zero.
+__global__ void k_assemble(const int8_t *mask, const float *rin, const float *rout, const float *tau,
+                           __nv_bfloat16 *y, int N, int H, int W, int C)
+{
+    const long long total = (long long)N * H * W;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total; p += (long long)gridDim.x * blockDim.x) {
+        const int n = (int)(p / ((long long)H * W));
+        const float v[4] = { (float)mask[p], (rin[n] - 1.f) * 20.f, (rout[n] - 1.f) * 20.f, (tau[n] - 0.75f) * 4.f };
+        for (int c = 0; c < C; ++c) y[p * C + c] = __float2bfloat16_rn(c < 4 ? v[c] : 0.f);
+    }
+}
+
+int grid_for(long long n) { return (int)((n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16); }
+
+template <int MODE>
+int run_conv(ConvArgs a, cudaStream_t s)
+{
+    dim3 grid((a.M + BM - 1) / BM, (a.Ncols + BN - 1) / BN, 1);
+    if (MODE == WGRAD) {
+        const int splits = 152 * 2 / max(1, (int)(grid.x * grid.y)) + 1;
+        a.k_chunk = ((a.K + splits - 1) / splits + BK - 1) / BK * BK;
+        grid.z = (a.K + a.k_chunk - 1) / a.k_chunk;
+    }
+    k_conv<MODE><<<grid, THREADS, 0, s>>>(a);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
+int plbm_nn_conv_fwd(const void *x, const void *w, const float *bias, void *y, int N, int H, int W, int Cin,
+                     int Cout, int relu, void *stream)
+{
+    ConvArgs a{};
+    a.x = (const __nv_bfloat16 *)x; a.w = (const __nv_bfloat16 *)w; a.bias = bias; a.y = (__nv_bfloat16 *)y;
+    a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout; a.relu = relu;
+    a.M = N * H * W; a.Ncols = Cout; a.K = 9 * Cin;
+    return run_conv<FWD>(a, (cudaStream_t)stream);
+}
+
+int plbm_nn_conv_dgrad(const void *g, const void *w, void *gx, int N, int H, int W, int Cin, int Cout, void *stream)
+{
+    ConvArgs a{};
+    a.g = (const __nv_bfloat16 *)g; a.w = (const __nv_bfloat16 *)w; a.y = (__nv_bfloat16 *)gx;
+    a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout;
+    a.M = N * H * W; a.Ncols = Cin; a.K = 9 * Cout;
+    return run_conv<DGRAD>(a, (cudaStream_t)stream);
+}
+
+int plbm_nn_conv_wgrad(const void *x, const void *g, float *gw, float *gb, int N, int H, int W, int Cin, int Cout,
+                       void *stream)
+{
+    ConvArgs a{};
+    a.x = (const __nv_bfloat16 *)x; a.g = (const __nv_bfloat16 *)g; a.gw = gw;
+    a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout;
+    a.M = Cout; a.Ncols = 9 * Cin; a.K = N * H * W;
+    int rc = run_conv<WGRAD>(a, (cudaStream_t)stream);
+    if (rc == PLBM_OK && gb) {
+        const long long P = (long long)N * H * W;
+        const long long gx = (P + 7) / 8 < 1024 ? (P + 7) / 8 : 1024;
+        dim3 grid((unsigned)gx, (unsigned)((Cout + 31) / 32));
+        k_bias_grad<<<grid, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)g, gb, P, Cout);
+        rc = cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+    }
+    return rc;
+}
+
+int plbm_nn_relu_bwd(const void *y, void *g, long long n, void *stream)
+{
+    k_relu_bwd<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)y, (__nv_bfloat16 *)g, n);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+int plbm_nn_pool2(const void *x, void *y, int N, int H, int W, int C, void *stream)
+{
+    k_pool2<<<grid_for((long long)N * H * W * C / 4), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)x,
+                                                                                       (__nv_bfloat16 *)y, N, H, W, C);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+int plbm_nn_pool2_bwd(const void *gy, void *gx, int N, int H, int W, int C, void *stream)
+{
+    k_pool2_bwd<<<grid_for((long long)N * H * W * C), 256, 0, (cudaStream_t)stream>>>(
+        (const __nv_bfloat16 *)gy, (__nv_bfloat16 *)gx, N, H, W, C);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+int plbm_nn_up2(const void *x, void *y, int N, int H, int W, int C, void *stream)
+{
+    k_up2<<<grid_for((long long)N * H * W * C), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)x,
+                                                                                 (__nv_bfloat16 *)y, N, H, W, C);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+int plbm_nn_up2_bwd(const void *gy, void *gx, int N, int H, int W, int C, void *stream)
+{
+    k_up2_bwd<<<grid_for((long long)N * H * W * C), 256, 0, (cudaStream_t)stream>>>(
+        (const __nv_bfloat16 *)gy, (__nv_bfloat16 *)gx, N, H, W, C);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+int plbm_nn_add(const void *a, const void *b, void *y, long long n, void *stream)
+{
+    k_add<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)a, (const __nv_bfloat16 *)b,
+                                                         (__nv_bfloat16 *)y, n);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+int plbm_nn_mse(const void *pred, const float *target, const int8_t *mask, void *grad, float *loss, long long P, int C,
+                float inv_count, void *stream)
+{
+    k_mse<<<grid_for(P * C), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)pred, target, mask,
+                                                             (__nv_bfloat16 *)grad, loss, P, C, inv_count);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+int plbm_nn_adam(float *w, const float *g, float *m, float *v, void *wb, long long n, float lr, float b1, float b2,
+                 float eps, int t, void *stream)
+{
+    const float c1 = 1.f / (1.f - powf(b1, (float)t)), c2 = 1.f / (1.f - powf(b2, (float)t));
+    k_adam<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(w, g, m, v, (__nv_bfloat16 *)wb, n, lr, b1, b2, eps, c1, c2);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+int plbm_nn_assemble(const int8_t *mask, const float *rin, const float *rout, const float *tau, void *y, int N, int H,
+                     int W, int C, void *stream)
+{
+    k_assemble<<<grid_for((long long)N * H * W), 256, 0, (cudaStream_t)stream>>>(mask, rin, rout, tau,
+                                                                                 (__nv_bfloat16 *)y, N, H, W, C);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -202,4 +202,42 @@ cudaError_t launch_residual(const double *jx, const double *jy, double *jx_prev,
     return cudaGetLastError();
 }
 
+template <int PREC, int L>
+__global__ void k_set_equilibrium(void *lat, StepParams p, const double *rho, const double *jx, const double *jy)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= p.W || y >= p.H) return;
+    const size_t r = (size_t)y * p.W + x;
+    const unsigned long long n = (unsigned long long)x + (unsigned long long)y * p.P;
+    const double R = rho[r], X = jx[r], Y = jy[r], usq = X * X + Y * Y;
+    for (int d = 0; d < 9; ++d) {
+        const double cu = (d % 3 - 1) * X + (d / 3 - 1) * Y;
+        const double w = p.weight[d];
+        const double f = w * (R + 3 * cu + 4.5 * cu * cu - 1.5 * usq);
+        typename Store<PREC>::C v;
+        if constexpr (PREC == F64_Q60) v = double_to_q(f);
+        else if constexpr (shifted<PREC>()) v = (float)(f - w);
+        else v = (typename Store<PREC>::C)f;
+        st<PREC>(lat, lidx<L>(n, d, p.N), d, v, p);
+    }
+}
+
+cudaError_t launch_set_equilibrium(void *lat, int prec, int lay, const StepParams &p, const double *rho,
+                                   const double *jx, const double *jy, cudaStream_t s)
+{
+    const dim3 grid((p.W + 127) / 128, p.H), block(128);
+#define PLBM_EQ(PR)                                                                                       \
+    case PR:                                                                                              \
+        if (lay == COLLISION) k_set_equilibrium<PR, COLLISION><<<grid, block, 0, s>>>(lat, p, rho, jx, jy); \
+        else if (lay == STREAM) k_set_equilibrium<PR, STREAM><<<grid, block, 0, s>>>(lat, p, rho, jx, jy);  \
+        else k_set_equilibrium<PR, BUNDLE><<<grid, block, 0, s>>>(lat, p, rho, jx, jy);                   \
+        break;
+    switch (prec) {
+        PLBM_EQ(F64_STRICT) PLBM_EQ(F64_FAST) PLBM_EQ(F32_REF) PLBM_EQ(F32) PLBM_EQ(F16S) PLBM_EQ(BF16S) PLBM_EQ(F64_Q60)
+    default: return cudaErrorInvalidValue;
+    }
+#undef PLBM_EQ
+    return cudaGetLastError();
+}
+
 }  // namespace plbm

@@ -1,0 +1,106 @@
+"""The neural operator's tensor-core kernels (plbm_nn_* in include/plbm_c.h) against the float64
+CPU reference (oracle/nn_ref.py) on bfloat16-rounded operands.  Tolerance: outputs are rounded to
+bfloat16 (relative 2^-8), so |gpu - ref| <= 1e-2 * max|ref| + 1e-3; weight gradients accumulate in
+FP32 and must agree to 1e-3 relative."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import nn_ref
+
+pytestmark = pytest.mark.gpu
+
+
+def _lib(plbm):
+    lib = plbm.load_library()
+    vp, i = ctypes.c_void_p, ctypes.c_int
+    lib.plbm_nn_conv_fwd.argtypes = [vp, vp, vp, vp, i, i, i, i, i, i, vp]
+    lib.plbm_nn_conv_dgrad.argtypes = [vp, vp, vp, i, i, i, i, i, vp]
+    lib.plbm_nn_conv_wgrad.argtypes = [vp, vp, vp, vp, i, i, i, i, i, vp]
+    lib.plbm_nn_pool2.argtypes = [vp, vp, i, i, i, i, vp]
+    lib.plbm_nn_up2.argtypes = [vp, vp, i, i, i, i, vp]
+    lib.plbm_nn_pool2_bwd.argtypes = [vp, vp, i, i, i, i, vp]
+    lib.plbm_nn_up2_bwd.argtypes = [vp, vp, i, i, i, i, vp]
+    return lib
+
+
+def _bf(t):
+    import torch
+    return torch.tensor(t, dtype=torch.float32).to(torch.bfloat16).cuda()
+
+
+def _np(t):
+    return t.float().cpu().numpy().astype(np.float64)
+
+
+def _close(got, ref, rel=1e-2):
+    assert np.max(np.abs(got - ref)) <= rel * np.max(np.abs(ref)) + 1e-3
+
+
+@pytest.mark.parametrize("n,h,w,cin,cout", [(2, 16, 24, 4, 32), (1, 32, 32, 32, 64), (2, 8, 16, 96, 128),
+                                           (1, 16, 16, 64, 3)])
+def test_conv_forward_and_gradients(plbm, n, h, w, cin, cout):
+    import torch
+    lib = _lib(plbm)
+    rng = np.random.default_rng(n * 1000 + cin)
+    x = nn_ref.bf16_round(rng.standard_normal((n, h, w, cin)))
+    wt = nn_ref.bf16_round(rng.standard_normal((cout, 9 * cin)) / np.sqrt(9 * cin))
+    b = rng.standard_normal(cout).astype(np.float32)
+    g = nn_ref.bf16_round(rng.standard_normal((n, h, w, cout)))
+    xd, wd, gd = _bf(x), _bf(wt), _bf(g)
+    bd = torch.tensor(b).cuda()
+    y = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
+    gx = torch.empty((n, h, w, cin), dtype=torch.bfloat16, device="cuda")
+    gw = torch.zeros((cout, 9 * cin), dtype=torch.float32, device="cuda")
+    gb = torch.zeros(cout, dtype=torch.float32, device="cuda")
+    for relu in (0, 1):
+        assert lib.plbm_nn_conv_fwd(xd.data_ptr(), wd.data_ptr(), bd.data_ptr(), y.data_ptr(), n, h, w, cin, cout,
+                                    relu, None) == 0
+        torch.cuda.synchronize()
+        _close(_np(y), nn_ref.conv_fwd(x, wt, b.astype(np.float64), bool(relu)))
+    assert lib.plbm_nn_conv_dgrad(gd.data_ptr(), wd.data_ptr(), gx.data_ptr(), n, h, w, cin, cout, None) == 0
+    assert lib.plbm_nn_conv_wgrad(xd.data_ptr(), gd.data_ptr(), gw.data_ptr(), gb.data_ptr(), n, h, w, cin, cout,
+                                  None) == 0
+    torch.cuda.synchronize()
+    _close(_np(gx), nn_ref.conv_dgrad(g, wt, cin))
+    rgw, rgb = nn_ref.conv_wgrad(x, g)
+    assert np.max(np.abs(_np(gw) - rgw)) <= 1e-3 * np.max(np.abs(rgw))
+    assert np.max(np.abs(_np(gb) - rgb)) <= 1e-2 * np.max(np.abs(rgb)) + 1e-2
+
+
+def test_pool_and_upsample(plbm):
+    import torch
+    lib = _lib(plbm)
+    rng = np.random.default_rng(3)
+    x = nn_ref.bf16_round(rng.standard_normal((2, 8, 12, 16)))
+    xd = _bf(x)
+    p = torch.empty((2, 4, 6, 16), dtype=torch.bfloat16, device="cuda")
+    u = torch.empty((2, 16, 24, 16), dtype=torch.bfloat16, device="cuda")
+    gp = torch.empty((2, 8, 12, 16), dtype=torch.bfloat16, device="cuda")
+    gu = torch.empty((2, 4, 6, 16), dtype=torch.bfloat16, device="cuda")
+    assert lib.plbm_nn_pool2(xd.data_ptr(), p.data_ptr(), 2, 8, 12, 16, None) == 0
+    assert lib.plbm_nn_up2(xd.data_ptr(), u.data_ptr(), 2, 16, 24, 16, None) == 0
+    assert lib.plbm_nn_pool2_bwd(p.data_ptr(), gp.data_ptr(), 2, 8, 12, 16, None) == 0
+    assert lib.plbm_nn_up2_bwd(xd.data_ptr(), gu.data_ptr(), 2, 4, 6, 16, None) == 0
+    torch.cuda.synchronize()
+    _close(_np(p), nn_ref.pool2(x))
+    assert np.array_equal(_np(u), nn_ref.up2(x))
+    # adjoints: <pool(x), y> = <x, pool_bwd(y)> and <up(x), z> = <x, up_bwd(z)>
+    _close(_np(gp), nn_ref.up2(_np(p)) / 4.0)
+    _close(_np(gu), nn_ref.pool2(x) * 4.0)
+
+
+def test_operator_trains_on_solver_steady_states(plbm):
+    """A short training run on 32 solver steady states (64x64) lowers the loss, and the prediction
+    initialises a handler that still reaches residual 1e-6."""
+    from portlbm_gb300 import warmstart as ws
+    data = ws.generate_dataset(32, 64, 64, seed=3, steps=3000, per_batch=32)
+    model = ws.NeuralOperator(seed=1)
+    hist = ws.train(model, data, epochs=6, batch=8, lr=3e-3)
+    assert hist["loss_history"][-1] < hist["loss_history"][0]
+    chan = data[0]
+    pred = model.predict(chan["mask"], chan["rin"], chan["rout"], chan["tau"])
+    assert all(np.all(np.isfinite(a)) for a in pred)
+    res = ws.solve(chan, init=pred, max_steps=100000)
+    assert res["residual"] < 1e-6

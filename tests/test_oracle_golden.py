@@ -69,3 +69,13 @@ def test_all_variants_agree(golden):
     for alg in ("nptl", "lptl", "npol", "nsol"):
         for lay in ("collision", "stream", "bundle"):
             assert np.array_equal(golden[f"variant_{alg}_{lay}__jx"], base)
+
+
+def test_nn_reference_adjoints():
+    """The CPU conv reference is self-consistent: <conv(x), g> = <x, dgrad(g)> = <w, wgrad(x, g)>."""
+    from oracle import nn_ref
+    rng = np.random.default_rng(0)
+    x, w, g = rng.standard_normal((2, 5, 6, 3)), rng.standard_normal((4, 27)), rng.standard_normal((2, 5, 6, 4))
+    a = (nn_ref.conv_fwd(x, w) * g).sum()
+    assert np.isclose(a, (x * nn_ref.conv_dgrad(g, w, 3)).sum())
+    assert np.isclose(a, (w * nn_ref.conv_wgrad(x, g)[0]).sum())
