@@ -63,8 +63,9 @@ def _ok(rc):
 class ConvLayer:
     def __init__(self, cin, cout, relu, rng, torch):
         self.cin, self.cout, self.relu = cin, cout, relu
-        w = rng.standard_normal((cout, 9 * cin)).astype(np.float32) * np.sqrt(2.0 / (9 * cin))
+        w = (rng.standard_normal((cout, 9 * cin)) * np.sqrt(2.0 / (9 * cin))).astype(np.float32)
         self.w = torch.from_numpy(w).cuda()                        # FP32 master
+        assert self.w.dtype == torch.float32
         self.wb = self.w.to(torch.bfloat16)                         # BF16 copy used by the kernels
         self.b = torch.zeros(cout, dtype=torch.float32, device="cuda")
         self.gw = torch.zeros_like(self.w)
