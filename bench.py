@@ -358,6 +358,12 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=0, help="CPU-baseline sample steps (0: auto)")
     ap.add_argument("--kernel-only", action="store_true", help="only the device-resident timed region (profiling)")
     ap.add_argument("--no-study", action="store_true", help="skip the precision study")
+    ap.add_argument("--warmstart-study", action="store_true",
+                    help="only the learned warm-start study: train on 2000 solver steady states (256x256), "
+                         "then time-to-residual 1e-6 from rest vs from the prediction on 200 held-out channels")
+    ap.add_argument("--warmstart-train", type=int, default=2000)
+    ap.add_argument("--warmstart-test", type=int, default=200)
+    ap.add_argument("--warmstart-save", default=None, help="write the trained weights (.npz) here")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -368,6 +374,15 @@ def main():
     import portlbm_gb300 as plbm
     from portlbm_gb300 import build as b
     b.build()
+    if args.warmstart_study:
+        if rank == 0:
+            from portlbm_gb300 import warmstart
+            t0 = time.perf_counter()
+            res = warmstart.study(n_train=args.warmstart_train, n_test=args.warmstart_test,
+                                  save=args.warmstart_save, log=lambda m: print(m, file=sys.stderr, flush=True))
+            res["wall_s"] = round(time.perf_counter() - t0, 1)
+            print(json.dumps({"warmstart_study": res}), flush=True)
+        return
     w, h = args.width, args.height
     mask = circle_channel_mask(w, h)
     pk = peaks()

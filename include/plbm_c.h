@@ -196,7 +196,9 @@ const char *plbm_noalloc_last_error(void);
 
 /* Runs the loop in chunks of K steps until the residual
  *   r = ||j^n - j^(n-K)||_2 / (K ||j^n||_2)   over fluid nodes (FP64 reductions on the GPU)
- * falls below `target` or `max_steps` is reached; writes the steps taken and the last residual.
+ * falls below `target` or `max_steps` is reached; writes the steps taken and the last residual
+ * (INFINITY when no window had a snapshot from exactly K steps before it: the snapshot carries
+ * over from the previous call and is dropped by plbm_set_equilibrium and re-initialisation).
  * Results on the host are those of the last step. */
 int plbm_run_to_residual(plbm_handler *h, double target, unsigned K, unsigned max_steps, unsigned *steps,
                          double *residual);
@@ -261,8 +263,9 @@ int plbm_nn_mse(const void *pred, const float *target, const int8_t *mask, void 
                 float inv_count, void *stream);
 int plbm_nn_adam(float *w, const float *g, float *m, float *v, void *w_bf16, long long n, float lr, float b1, float b2,
                  float eps, int t, void *stream);
-int plbm_nn_assemble(const int8_t *mask, const float *inlet_density, const float *outlet_density,
-                     const float *relaxation_time, void *y, int N, int H, int W, int C, void *stream);
+/* Network input [N,H,W,C] (C >= 4): channel 0 the int8 solid mask, channels 1..3 the per-sample
+ * scalars features[3n..3n+2] as constant planes, further channels zero. */
+int plbm_nn_assemble(const int8_t *mask, const float *features, void *y, int N, int H, int W, int C, void *stream);
 
 /* Last error message for h (or of the last failed create when h is NULL). */
 const char *plbm_last_error(const plbm_handler *h);

@@ -114,6 +114,7 @@ _SIGS = {
     "plbm_mass_momentum": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "plbm_compute_domain": (ctypes.c_int, [ctypes.POINTER(_CProps), ctypes.POINTER(ctypes.c_uint)]),
     "plbm_make_flags": (ctypes.c_int, [ctypes.POINTER(_CProps), ctypes.c_void_p]),
+    "plbm_set_equilibrium": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "plbm_run_to_residual": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_uint, ctypes.c_uint,
                                             ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_double)]),
     "plbm_porous_disks": (ctypes.c_int, [ctypes.c_uint, ctypes.c_uint, ctypes.c_uint64, ctypes.c_double,
@@ -370,6 +371,17 @@ class AlgorithmHandler:
 
     def sync_results(self) -> None:
         self._call("plbm_sync_results")
+
+    def set_equilibrium(self, rho, jx, jy) -> None:
+        """Replaces the state by the equilibrium populations of the inner fields (W*H each, row-major;
+        solid entries ignored); nptl/lptl only, before stepping or after an even number of steps."""
+        h, v = ctypes.c_uint(), ctypes.c_uint()
+        self._call("plbm_get_extents", ctypes.byref(h), ctypes.byref(v))
+        n = (h.value - 2) * (v.value - 2)
+        arrs = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in (rho, jx, jy)]
+        if any(a.size != n for a in arrs):
+            raise ValueError(f"fields must hold {n} inner values each")
+        self._call("plbm_set_equilibrium", *(a.ctypes.data for a in arrs))
 
     def mass_momentum(self) -> tuple:
         out = (ctypes.c_double * 3)()

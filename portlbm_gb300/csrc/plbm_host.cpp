@@ -405,6 +405,7 @@ struct plbm_handler {
     double *red_d = nullptr;
     int *status_d = nullptr;
     double *jprev_d = nullptr;   // 2 * W*H: j of the previous residual evaluation
+    long long jprev_iter = -1;   // iteration at which jprev_d was taken (-1: none)
     double *res_h[4] = { nullptr, nullptr, nullptr, nullptr };
     size_t nres = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -459,7 +460,7 @@ struct plbm_handler {
     void build()
     {
         release();
-        iteration = 0; progress = 0.0; frametime = 1.7976931348623157e308;
+        iteration = 0; progress = 0.0; frametime = 1.7976931348623157e308; jprev_iter = -1;
         stop = false; active = false; future_valid = true; worker_status = PLBM_OK; worker_error.clear();
         JsonExtras ex;
         if (from_json) props = json_to_props(settings_path, 0, &ex);
@@ -999,9 +1000,9 @@ int plbm_run_to_residual(plbm_handler *h, double target, unsigned K, unsigned ma
         }
         unsigned done = 0;
         double r = INFINITY;
-        bool first = true;
         while (done < max_steps) {
             const unsigned n = std::min(K, max_steps - done);
+            const long long before = (long long)h->iteration.load();
             double ms = 0;
             const int rc = plbm_run_steps(h, n, &ms);
             if (rc != PLBM_OK) throw Status{ rc, h->last_error };
@@ -1011,8 +1012,10 @@ int plbm_run_to_residual(plbm_handler *h, double target, unsigned K, unsigned ma
                                              h->nres, h->red_d, h->stream), "residual");
             cuda_check(cudaMemcpyAsync(sums, h->red_d, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "D2H");
             cuda_check(cudaStreamSynchronize(h->stream), "residual");
-            if (!first && n == K) r = sums[1] > 0 ? std::sqrt(sums[0]) / ((double)K * std::sqrt(sums[1])) : INFINITY;
-            first = false;
+            // a residual needs the snapshot of exactly K steps earlier (possibly from the previous call)
+            if (n == K && h->jprev_iter == before)
+                r = sums[1] > 0 ? std::sqrt(sums[0]) / ((double)K * std::sqrt(sums[1])) : INFINITY;
+            h->jprev_iter = (long long)h->iteration.load();
             if (r < target) break;
         }
         h->copy_results();
@@ -1094,12 +1097,19 @@ int plbm_set_equilibrium(plbm_handler *h, const double *rho, const double *jx, c
                                        h->stream), "H2D fields");
         cuda_check(plbm::launch_set_equilibrium(h->lat[par], h->prec, h->lay, h->base, tmp, tmp + h->nres,
                                                 tmp + 2 * h->nres, h->stream), "equilibrium");
-        // the outlet reads the previous step's jy of column x' = W-2
+        // the outlet reads the previous step's jy of column x' = W-2; steps never write it for a
+        // solid node there, so those entries keep the zero a rest start holds
+        if (h->W < 2) { cuda_check(cudaStreamSynchronize(h->stream), "equilibrium"); h->jprev_iter = -1; return; }
+        std::vector<int8_t> solid(h->H);
+        cuda_check(cudaMemcpy2DAsync(solid.data(), 1, h->flags_d + (h->W - 2), h->W, 1, h->H, cudaMemcpyDeviceToHost,
+                                     h->stream), "D2H flags");
+        cuda_check(cudaStreamSynchronize(h->stream), "flags");
         std::vector<double> col(h->H);
-        for (int y = 0; y < h->H; ++y) col[y] = jy[(size_t)y * h->W + h->W - 2];
+        for (int y = 0; y < h->H; ++y) col[y] = solid[y] ? 0.0 : jy[(size_t)y * h->W + h->W - 2];
         cuda_check(cudaMemcpyAsync(h->jy_d + (size_t)par * h->H, col.data(), h->H * sizeof(double),
                                    cudaMemcpyHostToDevice, h->stream), "H2D jy");
         cuda_check(cudaStreamSynchronize(h->stream), "equilibrium");
+        h->jprev_iter = -1;
     });
 }
 

@@ -271,15 +271,14 @@ __global__ void k_adam(float *w, const float *g, float *m, float *v, __nv_bfloat
     }
 }
 
-// Network input: channel 0 fluid(0)/solid(1) mask, then inlet density, outlet density and
-// relaxation time as constant planes (each shifted/scaled to O(1)); channels beyond 4 are zero.
-__global__ void k_assemble(const int8_t *mask, const float *rin, const float *rout, const float *tau,
-                           __nv_bfloat16 *y, int N, int H, int W, int C)
+// Network input: channel 0 fluid(0)/solid(1) mask, channels 1..3 the per-sample scalars
+// features[n][0..2] as constant planes; channels beyond 4 are zero.
+__global__ void k_assemble(const int8_t *mask, const float *features, __nv_bfloat16 *y, int N, int H, int W, int C)
 {
     const long long total = (long long)N * H * W;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total; p += (long long)gridDim.x * blockDim.x) {
         const int n = (int)(p / ((long long)H * W));
-        const float v[4] = { (float)mask[p], (rin[n] - 1.f) * 20.f, (rout[n] - 1.f) * 20.f, (tau[n] - 0.75f) * 4.f };
+        const float v[4] = { (float)mask[p], features[3 * n], features[3 * n + 1], features[3 * n + 2] };
         for (int c = 0; c < C; ++c) y[p * C + c] = __float2bfloat16_rn(c < 4 ? v[c] : 0.f);
     }
 }
@@ -397,11 +396,11 @@ int plbm_nn_adam(float *w, const float *g, float *m, float *v, void *wb, long lo
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
 }
 
-int plbm_nn_assemble(const int8_t *mask, const float *rin, const float *rout, const float *tau, void *y, int N, int H,
-                     int W, int C, void *stream)
+int plbm_nn_assemble(const int8_t *mask, const float *features, void *y, int N, int H, int W, int C, void *stream)
 {
-    k_assemble<<<grid_for((long long)N * H * W), 256, 0, (cudaStream_t)stream>>>(mask, rin, rout, tau,
-                                                                                 (__nv_bfloat16 *)y, N, H, W, C);
+    if (N <= 0 || H <= 0 || W <= 0 || C < 4) return PLBM_ERR_ARGUMENT;
+    k_assemble<<<grid_for((long long)N * H * W), 256, 0, (cudaStream_t)stream>>>(mask, features, (__nv_bfloat16 *)y,
+                                                                                 N, H, W, C);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
 }
 

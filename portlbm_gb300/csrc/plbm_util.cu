@@ -209,7 +209,9 @@ __global__ void k_set_equilibrium(void *lat, StepParams p, const double *rho, co
     if (x >= p.W || y >= p.H) return;
     const size_t r = (size_t)y * p.W + x;
     const unsigned long long n = (unsigned long long)x + (unsigned long long)y * p.P;
-    const double R = rho[r], X = jx[r], Y = jy[r], usq = X * X + Y * Y;
+    // solid nodes get the rest state, as at initialisation (their populations are never read)
+    const bool fluid = (p.links[n] & LINK_FLUID) != 0;
+    const double R = fluid ? rho[r] : 1.0, X = fluid ? jx[r] : 0.0, Y = fluid ? jy[r] : 0.0, usq = X * X + Y * Y;
     for (int d = 0; d < 9; ++d) {
         const double cu = (d % 3 - 1) * X + (d / 3 - 1) * Y;
         const double w = p.weight[d];

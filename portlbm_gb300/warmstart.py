@@ -10,7 +10,19 @@ tensor-core kernels in csrc/plbm_nn.cu; torch only provides device buffers):
 
     encoder  4->32->32 | pool | 32->64->64 | pool | 64->96->96 | pool | 96->128->128 | pool | 128->128->128
     decoder  per level: nearest x2, conv to the level's width (ReLU), + encoder skip, conv (ReLU)
-    head     32->3   (targets: (rho - 1) and j, each divided by its training-set std)
+    head     32->3
+
+Inputs are the solid mask and three per-sample scalars (a constant 1, which marks the domain
+edges through the zero padding, the relaxation time and the log of the Stokes velocity scale).
+Targets are made independent of the pressure drop, viscosity and channel length: with
+G = (rho_in - rho_out)/(W + 1) the mean density gradient and nu = (tau - 1/2)/3,
+
+    t_rho = (rho - rho_lin(x)) / G          rho_lin the linear profile between the ghost columns
+    t_j   = j * nu / (c_s^2 * G)            the Darcy-scaled momentum
+
+each divided by its training-set standard deviation.  At inference a 1-D series-resistance pass
+(`series_profile`) rescales the columns so the column mass fluxes agree, which sets the
+channel-scale density profile that a finite receptive field cannot see.
 
 Training data are steady states the solver itself produces (batches of porous channels,
 csrc/plbm_batch.cu), see `generate_dataset`.
@@ -46,13 +58,51 @@ def _fns():
         "plbm_nn_add": [vp, vp, vp, ll, vp],
         "plbm_nn_mse": [vp, vp, vp, vp, vp, ll, i, f, vp],
         "plbm_nn_adam": [vp, vp, vp, vp, vp, ll, f, f, f, f, i, vp],
-        "plbm_nn_assemble": [vp, vp, vp, vp, vp, i, i, i, i, vp],
-        "plbm_set_equilibrium": [vp, vp, vp, vp],
+        "plbm_nn_assemble": [vp, vp, vp, i, i, i, i, vp],
     }
     for name, args in sig.items():
         getattr(lib, name).argtypes = args
         getattr(lib, name).restype = ctypes.c_int
     return lib
+
+
+CS2 = 1.0 / 3.0
+STOKES_LENGTH = 8.0
+
+
+def channel_scales(w, rin, rout, tau):
+    """Mean density gradient G over the W + 1 links between the inlet and outlet ghost columns,
+    and the kinematic viscosity nu = (tau - 1/2)/3."""
+    return (rin - rout) / (w + 1), (tau - 0.5) / 3.0
+
+
+def linear_profile(w, rin, rout):
+    """Density of the straight profile at inner columns x = 0..W-1 (ghost x = -1 at rin, x = W at rout)."""
+    return rin - (rin - rout) * (np.arange(w) + 1.0) / (w + 1)
+
+
+def features(w, rin, rout, tau):
+    g, nu = channel_scales(w, rin, rout, tau)
+    u = CS2 * abs(g) * STOKES_LENGTH ** 2 / nu
+    return [1.0, (tau - 0.775) * 4.0, float(np.log10(max(u, 1e-12))) + 2.25]
+
+
+def series_profile(jx_pred, mask, w, rin, rout, sigma):
+    """Per-column gradient scale s(x) (mean 1) from the predicted column fluxes Q(x): in a steady
+    channel every column carries the same flux, so with local resistance 1/Q the gradient is
+    proportional to 1/Q (Q smoothed over `sigma` columns).  Returns s and the corrected profile
+    rho_b(x), or None when the prediction has no positive net flux everywhere."""
+    q = np.where(mask == 0, jx_pred, 0.0).sum(axis=0)
+    if sigma > 0:
+        r = int(3 * sigma)
+        k = np.exp(-0.5 * (np.arange(-r, r + 1) / sigma) ** 2)
+        q = np.convolve(np.pad(q, r, mode="reflect"), k / k.sum(), mode="valid")
+    if np.any(q <= 0):
+        return None
+    s = (1.0 / q) / np.mean(1.0 / q)
+    links = np.concatenate([[s[0]], 0.5 * (s[1:] + s[:-1]), [s[-1]]])      # W + 1 link gradients
+    drop = np.cumsum(links) / links.sum() * (rin - rout)
+    return s, rin - drop[:-1]
 
 
 def _ok(rc):
@@ -86,8 +136,28 @@ class NeuralOperator:
         self.dec = [ConvLayer(ci, co, True, rng, torch) for ci, co in DEC]
         self.head = ConvLayer(HEAD[0], HEAD[1], False, rng, torch)
         self.layers = self.enc + self.dec + [self.head]
-        self.scale = np.array([1.0, 1.0, 1.0], dtype=np.float32)
+        self.norm = np.array([1.0, 1.0])          # std of t_rho and of t_j over the training set
         self.step_count = 0
+
+    def save(self, path):
+        """Writes the FP32 master weights, biases and target scales to an .npz file."""
+        arrs = {"norm": self.norm}
+        for i, layer in enumerate(self.layers):
+            arrs[f"w{i}"] = layer.w.cpu().numpy()
+            arrs[f"b{i}"] = layer.b.cpu().numpy()
+        np.savez(path, **arrs)
+
+    def load(self, path):
+        z = np.load(path)
+        self.norm = z["norm"]
+        for i, layer in enumerate(self.layers):
+            w = self.torch.from_numpy(z[f"w{i}"].astype(np.float32))
+            if tuple(w.shape) != tuple(layer.w.shape):
+                raise ValueError(f"layer {i}: shape {tuple(w.shape)} != {tuple(layer.w.shape)}")
+            layer.w.copy_(w)
+            layer.wb.copy_(layer.w.to(self.torch.bfloat16))
+            layer.b.copy_(self.torch.from_numpy(z[f"b{i}"].astype(np.float32)))
+        return self
 
     def _buf(self, n, h, w, c):
         return self.torch.empty((n, h, w, c), dtype=self.torch.bfloat16, device="cuda")
@@ -184,26 +254,37 @@ class NeuralOperator:
                                       layer.v[1].data_ptr(), None, layer.b.numel(), lr, b1, b2, eps, self.step_count,
                                       None))
 
-    def assemble(self, masks, rin, rout, tau):
+    def assemble(self, masks, feats):
+        """masks: [n,h,w] int8 device tensor; feats: n rows of `features` -> [n,h,w,4] bf16 input."""
         torch = self.torch
         n, h, w = masks.shape
         x = self._buf(n, h, w, C_IN)
-        r1 = torch.tensor(rin, dtype=torch.float32, device="cuda")
-        r2 = torch.tensor(rout, dtype=torch.float32, device="cuda")
-        t = torch.tensor(tau, dtype=torch.float32, device="cuda")
-        _ok(self.lib.plbm_nn_assemble(masks.data_ptr(), r1.data_ptr(), r2.data_ptr(), t.data_ptr(), x.data_ptr(), n, h,
-                                      w, C_IN, None))
+        f = torch.tensor(np.asarray(feats, dtype=np.float32).reshape(n, 3), device="cuda")
+        _ok(self.lib.plbm_nn_assemble(masks.data_ptr(), f.data_ptr(), x.data_ptr(), n, h, w, C_IN, None))
         return x
 
-    def predict(self, mask: np.ndarray, rin: float, rout: float, tau: float):
-        """Predicted (rho, jx, jy) fields (float64, H*W) for one channel."""
+    def predict(self, mask: np.ndarray, rin: float, rout: float, tau: float, sigma: float = 16.0):
+        """Predicted steady (rho, jx, jy) fields (float64, H*W) for one channel; sigma < 0 skips
+        the series-resistance pass."""
         torch = self.torch
+        h, w = mask.shape
+        g, nu = channel_scales(w, rin, rout, tau)
+        if g == 0.0:
+            return np.full(h * w, rout), np.zeros(h * w), np.zeros(h * w)
         m = torch.from_numpy(np.ascontiguousarray(mask, dtype=np.int8)[None]).cuda()
-        x = self.assemble(m, [rin], [rout], [tau])
-        out = self.forward(x, 1, mask.shape[0], mask.shape[1]).float().cpu().numpy().reshape(-1, 3)
-        rho = 1.0 + out[:, 0] / self.scale[0]
-        jx, jy = out[:, 1] / self.scale[1], out[:, 2] / self.scale[2]
-        return rho.astype(np.float64), jx.astype(np.float64), jy.astype(np.float64)
+        x = self.assemble(m, [features(w, rin, rout, tau)])
+        out = self.forward(x, 1, h, w).float().cpu().numpy().astype(np.float64).reshape(h, w, 3)
+        t_rho = out[..., 0] * self.norm[0]
+        jscale = self.norm[1] * CS2 * g / nu
+        jx, jy = out[..., 1] * jscale, out[..., 2] * jscale
+        rho = linear_profile(w, rin, rout)[None, :] + g * t_rho
+        if sigma >= 0:
+            sp = series_profile(jx, mask, w, rin, rout, sigma)
+            if sp is not None:
+                s, rho_b = sp
+                rho = rho_b[None, :] + g * s[None, :] * t_rho
+                jx, jy = jx * s[None, :], jy * s[None, :]
+        return rho.reshape(-1), jx.reshape(-1), jy.reshape(-1)
 
 
 def random_channel(rng, w, h):
@@ -211,10 +292,20 @@ def random_channel(rng, w, h):
                 tau=float(rng.uniform(0.55, 1.0)), rin=float(rng.uniform(1.001, 1.05)), rout=1.0)
 
 
-def generate_dataset(n, w, h, seed, steps, per_batch=256, precision="f32"):
-    """n steady states of random porous channels from the batch solver (fixed `steps`)."""
+def converged_fields(mask, rho, jx, jy):
+    """False for a diverged run: BGK at relaxation times near 1/2 with a large inlet density can
+    blow up, and the NaN guard then leaves zeros (or a non-finite value) in the results."""
+    fl = mask.reshape(-1) == 0
+    return bool(np.all(np.isfinite(rho)) and np.all(np.isfinite(jx)) and np.all(np.isfinite(jy))
+                and np.all(rho[fl] > 0.5))
+
+
+def generate_dataset(n, w, h, seed, steps, per_batch=256, precision="f32", stats=None):
+    """n steady states of random porous channels from the batch solver (fixed `steps`); channels
+    whose run diverged are drawn again (their count goes to stats["diverged"])."""
     rng = np.random.default_rng(seed)
     samples = []
+    diverged = 0
     while len(samples) < n:
         k = min(per_batch, n - len(samples))
         chans = [random_channel(rng, w, h) for _ in range(k)]
@@ -224,28 +315,44 @@ def generate_dataset(n, w, h, seed, steps, per_batch=256, precision="f32"):
         b.run(steps, mode="persistent_graph")
         for i, c in enumerate(chans):
             c["rho"], c["jx"], c["jy"] = b.result(i, 0), b.result(i, 1), b.result(i, 2)
-            samples.append(c)
+            if converged_fields(c["mask"], c["rho"], c["jx"], c["jy"]):
+                samples.append(c)
+            else:
+                diverged += 1
         b.close()
+    if stats is not None:
+        stats["diverged"] = diverged
     return samples
 
 
-def train(model: NeuralOperator, samples, epochs=10, batch=16, lr=2e-3, log=None):
+def train(model: NeuralOperator, samples, epochs=10, batch=16, lr=2e-3, flip=True, log=None):
+    """Adam with a cosine learning rate over `epochs`; flip=True adds every sample mirrored about
+    the channel axis (y -> H-1-y, jy -> -jy), a symmetry of the walled channel."""
     torch = model.torch
     n = len(samples)
     h, w = samples[0]["mask"].shape
     masks_np = np.stack([s["mask"] for s in samples])
-    masks = torch.from_numpy(masks_np).cuda()
+    t_rho = np.empty((n, h, w))
+    t_j = np.empty((n, h, w, 2))
+    feats = np.empty((n, 3), dtype=np.float32)
+    for i, s in enumerate(samples):
+        g, nu = channel_scales(w, s["rin"], s["rout"], s["tau"])
+        t_rho[i] = (s["rho"].reshape(h, w) - linear_profile(w, s["rin"], s["rout"])[None, :]) / g
+        t_j[i, ..., 0] = s["jx"].reshape(h, w) * nu / (CS2 * g)
+        t_j[i, ..., 1] = s["jy"].reshape(h, w) * nu / (CS2 * g)
+        feats[i] = features(w, s["rin"], s["rout"], s["tau"])
+    if flip:
+        masks_np = np.concatenate([masks_np, masks_np[:, ::-1]])
+        t_rho = np.concatenate([t_rho, t_rho[:, ::-1]])
+        t_j = np.concatenate([t_j, t_j[:, ::-1] * np.array([1.0, -1.0])])
+        feats = np.concatenate([feats, feats])
+        n *= 2
+    masks = torch.from_numpy(np.ascontiguousarray(masks_np)).cuda()
     fl = masks_np.reshape(n, -1) == 0
-    drho = np.stack([s["rho"] - 1.0 for s in samples]).reshape(n, -1)
-    jx = np.stack([s["jx"] for s in samples]).reshape(n, -1)
-    jy = np.stack([s["jy"] for s in samples]).reshape(n, -1)
-    model.scale = np.array([1.0 / drho[fl].std(), 1.0 / np.concatenate([jx[fl], jy[fl]]).std(),
-                            1.0 / np.concatenate([jx[fl], jy[fl]]).std()], dtype=np.float32)
-    tgt = np.stack([drho * model.scale[0], jx * model.scale[1], jy * model.scale[2]], axis=-1).astype(np.float32)
-    targets = torch.from_numpy(tgt.reshape(n, h, w, 3)).cuda()
-    rin = np.array([s["rin"] for s in samples], dtype=np.float32)
-    rout = np.array([s["rout"] for s in samples], dtype=np.float32)
-    tau = np.array([s["tau"] for s in samples], dtype=np.float32)
+    fl3 = fl.reshape(n, h, w)
+    model.norm = np.array([t_rho[fl3].std(), t_j[fl3].std()])
+    tgt = np.concatenate([t_rho[..., None] / model.norm[0], t_j / model.norm[1]], axis=-1).astype(np.float32)
+    targets = torch.from_numpy(tgt).cuda()
     loss_d = torch.zeros(1, dtype=torch.float32, device="cuda")
     grad = torch.empty((batch, h, w, 3), dtype=torch.bfloat16, device="cuda")
     rng = np.random.default_rng(1)
@@ -259,8 +366,7 @@ def train(model: NeuralOperator, samples, epochs=10, batch=16, lr=2e-3, log=None
             sel = order[it * batch:(it + 1) * batch]
             idx = torch.from_numpy(sel).cuda()
             m = masks.index_select(0, idx).contiguous()
-            x = model.assemble(m, rin[order[it * batch:(it + 1) * batch]], rout[order[it * batch:(it + 1) * batch]],
-                               tau[order[it * batch:(it + 1) * batch]])
+            x = model.assemble(m, feats[sel])
             pred = model.forward(x, batch, h, w)
             t = targets.index_select(0, idx).contiguous()
             loss_d.zero_()
@@ -279,62 +385,130 @@ def train(model: NeuralOperator, samples, epochs=10, batch=16, lr=2e-3, log=None
 
 
 def solve(chan, precision="f64_q60", init=None, target=1e-6, k=100, max_steps=400000):
-    """Runs the plain solver to `target`; init = (rho, jx, jy) to start from their equilibrium."""
+    """Runs the plain solver to `target`; init = (rho, jx, jy) to start from their equilibrium.
+    The first residual is taken after 2k steps (the fallback comparison); wall time includes
+    loading the initial state."""
     h, w = chan["mask"].shape
     props = Properties("nptl", "stream", False, 1024, 10 ** 9, 10 ** 9, "Hagen-Poiseuille", h, w, 0.0, 0.0,
                        chan["rin"], 0.0, 0.0, chan["rout"], chan["tau"])
     hd = create_handler(props, precision=precision, mask=chan["mask"])
-    lib = load_library()
-    if init is not None:
-        rho, jx, jy = (np.ascontiguousarray(a, dtype=np.float64) for a in init)
-        rc = lib.plbm_set_equilibrium(hd._h, rho.ctypes.data, jx.ctypes.data, jy.ctypes.data)
-        if rc != 0:
-            raise RuntimeError("set_equilibrium failed")
     t0 = time.perf_counter()
-    steps, r = hd.run_to_residual(target, k, 2 * k)      # first residual: compares inits
-    first = r
+    if init is not None:
+        hd.set_equilibrium(*init)
+    steps, r = hd.run_to_residual(target, k, 2 * k)
+    first, first_s, first_steps = r, time.perf_counter() - t0, steps
     if r >= target:
         more, r = hd.run_to_residual(target, k, max_steps)
         steps += more
     dt = time.perf_counter() - t0
+    jx, jy = hd.get_x_velocities(), hd.get_y_velocities()
     hd.close()
-    return {"steps": steps, "seconds": dt, "first_residual": first, "residual": r}
+    return {"steps": steps, "seconds": dt, "first_residual": first, "first_seconds": first_s,
+            "first_steps": first_steps, "residual": r, "j": (jx, jy)}
 
 
-def study(n_train=2000, n_test=200, size=(256, 256), large=(1024, 256), steps=8000, large_steps=24000, epochs=12,
-          seed=7, log=None):
+def state_difference(mask, a, b):
+    """Relative L2 distance of two momentum fields over the fluid nodes."""
+    fl = mask.reshape(-1) == 0
+    num = np.sqrt(np.sum((a[0] - b[0])[fl] ** 2) + np.sum((a[1] - b[1])[fl] ** 2))
+    den = np.sqrt(np.sum(b[0][fl] ** 2) + np.sum(b[1][fl] ** 2))
+    return float(num / den) if den > 0 else float(num)
+
+
+def rest_ramp_init(chan):
+    """Initial state without the network: the straight density profile and zero momentum."""
+    h, w = chan["mask"].shape
+    return np.tile(linear_profile(w, chan["rin"], chan["rout"]), h), np.zeros(h * w), np.zeros(h * w)
+
+
+def evaluate(model, chans, sigma=16.0, ablation=True, log=None):
+    """Rest start vs warm start (with fallback) on each channel; time to residual 1e-6.  A channel
+    whose rest start diverges is reported with cold_steps None (excluded from the comparison); a
+    warm start that diverges counts as a fallback."""
+    rows = []
+    for chan in chans:
+        h, w = chan["mask"].shape
+        row = {"size": f"{w}x{h}", "tau": chan["tau"], "rin": chan["rin"]}
+        try:
+            cold = solve(chan)
+        except Exception:
+            row.update(cold_steps=None, fallback=None)
+            rows.append(row)
+            if log:
+                log(row)
+            continue
+        t0 = time.perf_counter()
+        pred = model.predict(chan["mask"], chan["rin"], chan["rout"], chan["tau"], sigma=sigma)
+        infer = time.perf_counter() - t0
+        try:
+            warm = solve(chan, init=pred)
+            fb = warm["first_residual"] > cold["first_residual"]
+        except Exception:
+            warm, fb = None, True
+        if fb:   # the warm start's probe phase was spent, then the rest start runs in full
+            probe_steps = warm["first_steps"] if warm else 0
+            probe_s = warm["first_seconds"] if warm else 0.0
+            w_steps, w_s = probe_steps + cold["steps"], infer + probe_s + cold["seconds"]
+        else:    # the rest start's probe phase was spent to decide
+            w_steps = warm["steps"] + cold["first_steps"]
+            w_s = infer + warm["seconds"] + cold["first_seconds"]
+        row.update(cold_steps=cold["steps"], cold_s=cold["seconds"], warm_steps=w_steps, warm_s=w_s, fallback=bool(fb),
+                   infer_s=infer, cold_r0=cold["first_residual"], warm_r0=warm["first_residual"] if warm else None,
+                   state_diff=state_difference(chan["mask"], warm["j"], cold["j"]) if warm else None)
+        if ablation:   # the same warm start from the straight profile alone (no network)
+            try:
+                ramp = solve(chan, init=rest_ramp_init(chan))
+                row.update(ramp_steps=ramp["steps"], ramp_s=ramp["seconds"])
+            except Exception:
+                row.update(ramp_steps=None, ramp_s=None)
+        rows.append(row)
+        if log:
+            log(row)
+    return rows
+
+
+def aggregate(rows):
+    diverged = sum(r["cold_steps"] is None for r in rows)
+    rows = [r for r in rows if r["cold_steps"] is not None]
+    if not rows:
+        return {"n": 0, "diverged": diverged}
+    cs = np.array([r["cold_steps"] for r in rows], dtype=float)
+    ws = np.array([r["warm_steps"] for r in rows], dtype=float)
+    ct = np.array([r["cold_s"] for r in rows])
+    wt = np.array([r["warm_s"] for r in rows])
+    return {"n": len(rows), "median_cold_steps": float(np.median(cs)), "median_warm_steps": float(np.median(ws)),
+            "steps_reduction_total": float(cs.sum() / ws.sum()), "time_reduction_total": float(ct.sum() / wt.sum()),
+            "time_reduction_median": float(np.median(ct / wt)), "cold_s_total": float(ct.sum()),
+            "warm_s_total": float(wt.sum()), "fallbacks": int(sum(r["fallback"] for r in rows)),
+            "ramp_only_steps_reduction_total": (float(cs.sum() / sum(r["ramp_steps"] for r in rows))
+                                                if all(r.get("ramp_steps") for r in rows) else None),
+            "max_state_diff": max((r["state_diff"] for r in rows if r["state_diff"] is not None), default=None),
+            "diverged": diverged}
+
+
+def study(n_train=2000, n_test=200, size=(256, 256), large=(1024, 256), steps=20000, epochs=16, seed=7,
+          sigma=16.0, save=None, log=None):
     """Trains on solver-generated steady states and measures steps / wall time to residual 1e-6
     from rest versus from the prediction on held-out geometries (half at `size`, half at `large`)."""
     t0 = time.perf_counter()
     w, h = size
-    data = generate_dataset(n_train, w, h, seed, steps)
+    gen = {}
+    data = generate_dataset(n_train, w, h, seed, steps, stats=gen)
     t_data = time.perf_counter() - t0
     model = NeuralOperator(seed)
     hist = train(model, data, epochs=epochs, log=log)
+    if save:
+        model.save(save)
+    del data
     rng = np.random.default_rng(seed + 99)
-    rows = []
-    for i in range(n_test):
-        ww, hh = size if i % 2 == 0 else large
-        chan = random_channel(rng, ww, hh)
-        cold = solve(chan)
-        ti = time.perf_counter()
-        pred = model.predict(chan["mask"], chan["rin"], chan["rout"], chan["tau"])
-        infer = time.perf_counter() - ti
-        warm = solve(chan, init=pred)
-        used = warm if warm["first_residual"] <= cold["first_residual"] else None
-        rows.append({"size": f"{ww}x{hh}", "cold_steps": cold["steps"], "cold_s": cold["seconds"],
-                     "warm_steps": warm["steps"], "warm_s": warm["seconds"] + infer, "fallback": used is None,
-                     "infer_s": infer})
-    def agg(sel):
-        cs = np.array([r["cold_steps"] for r in sel], dtype=float)
-        ws = np.array([r["cold_steps"] if r["fallback"] else r["warm_steps"] for r in sel], dtype=float)
-        ct = np.array([r["cold_s"] for r in sel])
-        wt = np.array([r["cold_s"] + r["warm_s"] if r["fallback"] else r["warm_s"] for r in sel])
-        return {"n": len(sel), "median_cold_steps": float(np.median(cs)), "median_warm_steps": float(np.median(ws)),
-                "steps_reduction_total": float(cs.sum() / ws.sum()), "time_reduction_total": float(ct.sum() / wt.sum()),
-                "fallbacks": int(sum(r["fallback"] for r in sel))}
-    return {"train": {"samples": n_train, "size": f"{w}x{h}", "solver_steps": steps, "dataset_s": round(t_data, 1),
-                      "epochs": epochs, "train_s": round(hist["seconds"], 1),
-                      "loss_first": hist["loss_history"][0], "loss_last": hist["loss_history"][-1]},
-            "held_out": {"all": agg(rows), f"{w}x{h}": agg([r for r in rows if r["size"] == f"{w}x{h}"]),
-                         f"{large[0]}x{large[1]}": agg([r for r in rows if r["size"] == f"{large[0]}x{large[1]}"])}}
+    chans = [random_channel(rng, *(size if i % 2 == 0 else large)) for i in range(n_test)]
+    rows = evaluate(model, chans, sigma=sigma, log=log)
+    out = {"train": {"samples": n_train, "size": f"{w}x{h}", "solver_steps": steps, "dataset_s": round(t_data, 1),
+                     "diverged_redrawn": gen["diverged"],
+                     "epochs": epochs, "train_s": round(hist["seconds"], 1),
+                     "loss_first": hist["loss_history"][0], "loss_last": hist["loss_history"][-1]},
+           "held_out": {"all": aggregate(rows)}}
+    for sz in (size, large):
+        key = f"{sz[0]}x{sz[1]}"
+        out["held_out"][key] = aggregate([r for r in rows if r["size"] == key])
+    return out

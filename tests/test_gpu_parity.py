@@ -135,6 +135,80 @@ def test_residual_decreases_and_steady_state_is_reached(plbm):
     assert np.all(np.isfinite(jx)) and jx[mask.reshape(-1) == 0].mean() > 0
 
 
+def test_residual_windows_chain_across_calls(plbm):
+    """The snapshot of one call is the baseline of the next: K-step calls report the same residuals
+    as one call over the same steps."""
+    mask = plbm.porous_disks(96, 40, 5, 0.7)
+    props = plbm.Properties("nptl", "stream", False, 64, 10 ** 6, 10 ** 6, "Hagen-Poiseuille", 40, 96, 0.0, 0.0,
+                            1.02, 0.0, 0.0, 1.0, 0.7)
+    a = plbm.create_handler(props, precision="f64_q60", mask=mask)
+    b = plbm.create_handler(props, precision="f64_q60", mask=mask)
+    s1, r1 = a.run_to_residual(0.0, 50, 50)
+    assert s1 == 50 and r1 == float("inf")          # no snapshot before the first window
+    s2, r2 = a.run_to_residual(0.0, 50, 50)
+    s3, r3 = b.run_to_residual(0.0, 50, 100)
+    assert s2 == 50 and s3 == 100 and np.isfinite(r2) and r2 == r3
+    a.close()
+    b.close()
+
+
+def _outlet_strip_mask(w, h):
+    """Walls on the first/last rows and a block reaching column W-2, leaving a one-node strip of
+    fluid in the outlet column beside it."""
+    m = np.zeros((h, w), dtype=np.int8)
+    m[0, :] = m[-1, :] = 1
+    m[4:h - 5, w - 9:w - 1] = 1
+    m[6:9, 10:14] = 1
+    return m
+
+
+@pytest.mark.parametrize("precision", ["f64_strict", "f64_q60", "f32"])
+def test_set_equilibrium_ignores_solid_entries(plbm, precision):
+    """Values at solid nodes, including column W-2 whose jy the outlet reads, do not reach the run."""
+    w, h = 48, 24
+    mask = _outlet_strip_mask(w, h)
+    props = plbm.Properties("nptl", "stream", False, 64, 10 ** 6, 10 ** 6, "Hagen-Poiseuille", h, w, 0.0, 0.0,
+                            1.02, 0.0, 0.0, 1.0, 0.8)
+    rng = np.random.default_rng(0)
+    x = np.arange(w)[None, :].repeat(h, 0)
+    clean = [(1.02 - 0.02 * (x + 1) / (w + 1)).ravel(), np.full(w * h, 2e-3), 1e-4 * rng.standard_normal(w * h)]
+    solid = mask.reshape(-1) == 1
+    for f in clean:
+        f[solid] = 0.0
+    dirty = [f.copy() for f in clean]
+    for f in dirty:
+        f[solid] = rng.uniform(-0.5, 0.5, solid.sum())
+    out = []
+    for fields in (clean, dirty):
+        hd = plbm.create_handler(props, precision=precision, mask=mask)
+        hd.set_equilibrium(*fields)
+        hd.run_steps(400)
+        hd.sync_results()
+        out.append([hd.get_densities().copy(), hd.get_x_velocities().copy(), hd.get_y_velocities().copy()])
+        hd.close()
+    for k in range(3):
+        assert np.array_equal(out[0][k], out[1][k]), k
+
+
+@pytest.mark.parametrize("precision", ["f64_strict", "f64_q60"])
+def test_set_equilibrium_of_rest_state_is_the_rest_start(plbm, precision):
+    """Loading rho = 1, j = 0 gives the same run as the handler's own initialisation."""
+    w, h = 48, 24
+    mask = _outlet_strip_mask(w, h)
+    props = plbm.Properties("nptl", "stream", False, 64, 10 ** 6, 10 ** 6, "Hagen-Poiseuille", h, w, 0.0, 0.0,
+                            1.02, 0.0, 0.0, 1.0, 0.8)
+    out = []
+    for load in (False, True):
+        hd = plbm.create_handler(props, precision=precision, mask=mask)
+        if load:
+            hd.set_equilibrium(np.ones(w * h), np.zeros(w * h), np.zeros(w * h))
+        hd.run_steps(300)
+        hd.sync_results()
+        out.append([hd.get_densities().copy(), hd.get_x_velocities().copy()])
+        hd.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
 def _batch_domains(plbm, n=5, seed=11):
     rng = np.random.default_rng(seed)
     doms = []
