@@ -147,7 +147,8 @@ def test_residual_windows_chain_across_calls(plbm):
     assert s1 == 50 and r1 == float("inf")          # no snapshot before the first window
     s2, r2 = a.run_to_residual(0.0, 50, 50)
     s3, r3 = b.run_to_residual(0.0, 50, 100)
-    assert s2 == 50 and s3 == 100 and np.isfinite(r2) and r2 == r3
+    # same fields; the FP64 sums are accumulated with atomics, so the order (last bits) may differ
+    assert s2 == 50 and s3 == 100 and np.isfinite(r2) and abs(r2 - r3) <= 1e-12 * r3
     a.close()
     b.close()
 
