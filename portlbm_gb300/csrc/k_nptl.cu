@@ -5,6 +5,13 @@
 namespace plbm {
 cudaError_t launch_nptl(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s)
 {
+    // 2-byte storage in the stream layout: vectorised rows (launch shape of its own)
+    if ((prec == F16S || prec == BF16S) && lay == STREAM) {
+        const dim3 vb(32, VEC_ROWS), vg((unsigned)((p.P + 32 * VEC - 1) / (32 * VEC)), (unsigned)((p.H + VEC_ROWS - 1) / VEC_ROWS));
+        if (prec == F16S) k_nptl_vec<F16S><<<vg, vb, 0, s>>>(p);
+        else k_nptl_vec<BF16S><<<vg, vb, 0, s>>>(p);
+        return cudaGetLastError();
+    }
     switch (prec * 3 + lay) {
         PLBM_ALL_CASES(k_nptl)
     default: return cudaErrorInvalidValue;

@@ -18,6 +18,7 @@
 // Layouts (access.hpp:102-172) apply unchanged to the inner grid: collision 9n+d, stream N*d+n,
 // bundle 3(d/3)N + d%3 + 3n.
 #pragma once
+#include <type_traits>
 
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -87,6 +88,9 @@ __device__ __forceinline__ void st(void *base, unsigned long long i, int d, type
 // ---- the BGK update ------------------------------------------------------------------------
 
 struct Moments { double rho, jx, jy, usq; };
+// The float forms keep their moments in float: GB300 issues FP64 at 1/64 of the FP32 rate, so
+// they are widened to double only on the steps that write them (observables<PREC>).
+struct MomentsF { float rho, jx, jy, usq; };
 
 __device__ __forceinline__ double nan_guard(double v)
 {
@@ -180,7 +184,7 @@ __device__ __forceinline__ Moments collide_f64_fast(double f[9], double omega)
 // F32_REF: the reference compiled with USE_FLOAT.  real_type is float, but the literals 9.0/2
 // and 3.0/2 are double, so the equilibrium bracket is evaluated in double and rounded to float
 // when assigned (nptl_kernels.hpp:401-402); every operation is rounded separately.
-__device__ __forceinline__ Moments collide_f32_ref(float f[9], float omega)
+__device__ __forceinline__ MomentsF collide_f32_ref(float f[9], float omega)
 {
     float rho = f[0];
 #pragma unroll
@@ -215,11 +219,11 @@ __device__ __forceinline__ Moments collide_f32_ref(float f[9], float omega)
     feq[8] = (float)__dmul_rn((double)w36, __dsub_rn(t3p[2], h));
 #pragma unroll
     for (int d = 0; d < 9; ++d) f[d] = __fadd_rn(__fmul_rn(nom, __fsub_rn(f[d], feq[d])), f[d]);
-    return { (double)rho, (double)jx, (double)jy, (double)usq };
+    return { rho, jx, jy, usq };
 }
 
 // FP32 arithmetic for the F32 / F16S / BF16S storage forms (same regrouping as F64_FAST).
-__device__ __forceinline__ Moments collide_f32(float f[9], float omega)
+__device__ __forceinline__ MomentsF collide_f32(float f[9], float omega)
 {
     const float A = f[2] + f[5] + f[8], B = f[0] + f[3] + f[6];
     const float C = f[6] + f[7] + f[8], E = f[0] + f[1] + f[2];
@@ -239,7 +243,7 @@ __device__ __forceinline__ Moments collide_f32(float f[9], float omega)
       f[8] = fmaf(odd, u, fmaf(om1, f[8], sym)); f[0] = fmaf(-odd, u, fmaf(om1, f[0], sym)); }
     { const float u = jx - jy, sym = fmaf(4.5f * ow36 * u, u, b36), odd = 3.0f * ow36;
       f[2] = fmaf(odd, u, fmaf(om1, f[2], sym)); f[6] = fmaf(-odd, u, fmaf(om1, f[6], sym)); }
-    return { (double)rho, (double)jx, (double)jy, (double)usq };
+    return { rho, jx, jy, usq };
 }
 
 // ---- F64_Q60: FP64-accuracy populations in 64-bit fixed point ------------------------------
@@ -354,7 +358,10 @@ __device__ __forceinline__ Moments collide_q60(long long f[9], const StepParams 
 }
 
 template <int PREC>
-__device__ __forceinline__ Moments collide(typename Store<PREC>::C f[9], const StepParams &p)
+using MomentsOf = typename std::conditional<sizeof(typename Store<PREC>::C) == 4, MomentsF, Moments>::type;
+
+template <int PREC>
+__device__ __forceinline__ MomentsOf<PREC> collide(typename Store<PREC>::C f[9], const StepParams &p)
 {
     if constexpr (PREC == F64_STRICT) return collide_f64_strict(f, p.omega);
     else if constexpr (PREC == F64_FAST) return collide_f64_fast(f, p.omega);
@@ -453,17 +460,18 @@ __device__ __forceinline__ void write_observables_f32ref(const Moments &m, int x
 }
 
 template <int PREC>
-__device__ __forceinline__ void observables(const Moments &m, int xi, int yi, const StepParams &p)
+__device__ __forceinline__ void observables(const MomentsOf<PREC> &m, int xi, int yi, const StepParams &p)
 {
+    if (!p.write_results && xi != p.W - 2) return;   // nothing is written on this step
     if constexpr (PREC == F32_REF) {
-        write_observables_f32ref(m, xi, yi, p);
+        const Moments d = { (double)m.rho, (double)m.jx, (double)m.jy, (double)m.usq };
+        write_observables_f32ref(d, xi, yi, p);
     } else if constexpr (PREC == F64_Q60) {
-        if (!p.write_results && xi != p.W - 2) return;
         const Moments d = { q_to_double(__double_as_longlong(m.rho)), q_to_double(__double_as_longlong(m.jx)),
                             q_to_double(__double_as_longlong(m.jy)), q_to_double(__double_as_longlong(m.usq)) };
         write_observables(d, xi, yi, p);
     } else if constexpr (shifted<PREC>()) {
-        const Moments d = { 1.0 + m.rho, m.jx, m.jy, m.usq };   // rho = 1 + drho
+        const Moments d = { 1.0 + (double)m.rho, (double)m.jx, (double)m.jy, (double)m.usq };   // rho = 1 + drho
         write_observables(d, xi, yi, p);
     } else {
         write_observables(m, xi, yi, p);

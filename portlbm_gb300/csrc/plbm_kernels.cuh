@@ -82,7 +82,7 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
     for (int j = 0; j < NY; ++j) {
         if (!(lk[j] & LINK_FLUID)) continue;
         if (is_outlet_row(xi[j], yi[j], p)) outlet_fill<PREC>(f[j], p.jy_prev[yi[j]], p);
-        const Moments m = collide<PREC>(f[j], p);
+        const auto m = collide<PREC>(f[j], p);
 #pragma unroll
         for (int d = 0; d < 9; ++d) st<PREC>(p.lat1, lidx<L>(n[j], d, p.N), d, f[j][d], p);
         observables<PREC>(m, xi[j], yi[j], p);
@@ -102,6 +102,142 @@ __global__ void k_nptl(StepParams p)
 #pragma unroll
     for (int j = 0; j < NY; ++j) { xi[j] = x; yi[j] = y0 + j; }
     update_two_lattice_rows<PREC, L, NY>(xi, yi, p);
+}
+
+// nptl, stream layout, 2-byte storage (F16S / BF16S): each thread updates VEC consecutive nodes
+// of one row with a single 16-byte load and store per population plane; a warp covers 256
+// consecutive nodes.  The value a node pulls across its vector's edge (x - 1 or x + 1) comes from
+// the neighbouring lane by a warp shuffle, or at the warp's edge from one 2-byte load.  Nodes
+// that are not interior fluid re-gather their populations with the scalar pull (bounce-back,
+// inlet/outlet and wall ghosts), so the arithmetic and the results are those of k_nptl.  Solid
+// nodes and row padding are written back as the rest state (df = 0), which is what they hold.
+constexpr int VEC = 8;
+constexpr int VEC_ROWS = 4;   // rows (warps) per block
+
+// Two packed 2-byte values <-> two floats with one conversion instruction each way; the same
+// values and round-to-nearest-even results as ld<PREC> / st<PREC>.
+template <int PREC> __device__ __forceinline__ float2 vec_unpack(unsigned w)
+{
+    if constexpr (PREC == F16S) {
+        __half2 h = *reinterpret_cast<__half2 *>(&w);
+        const float2 v = __half22float2(h);
+        return make_float2(v.x * F16_UNSCALE, v.y * F16_UNSCALE);
+    } else {
+        __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&w);
+        return __bfloat1622float2(h);
+    }
+}
+template <int PREC> __device__ __forceinline__ unsigned vec_pack(float lo, float hi)
+{
+    if constexpr (PREC == F16S) {
+        __half2 h = __floats2half2_rn(lo * F16_SCALE, hi * F16_SCALE);
+        return *reinterpret_cast<unsigned *>(&h);
+    } else {
+        __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+        return *reinterpret_cast<unsigned *>(&h);
+    }
+}
+
+// Writing the observables is a separate (not inlined) function taking the four moments by value,
+// so its FP64 widening is never scheduled into the interior path (GB300 issues FP64 at 1/64 of
+// the FP32 rate).
+template <int PREC>
+__device__ __forceinline__ void vec_edge_gather(float *f, int x, int y, uint16_t lk, const StepParams &p)
+{
+    const unsigned long long n = (unsigned long long)x + (unsigned long long)y * p.P;
+#pragma unroll
+    for (int d = 0; d < 9; ++d) f[d] = pull_one<PREC, STREAM>(p.lat0, n, x, y, d, lk, p);
+    if (is_outlet_row(x, y, p)) outlet_fill<PREC>(f, p.jy_prev[y], p);
+}
+
+template <int PREC>
+__device__ __noinline__ void vec_write_observables(MomentsF m, int x, int y, const StepParams &p)
+{
+    observables<PREC>(m, x, y, p);
+}
+
+template <int PREC>
+__device__ __forceinline__ void vec_node(float f[9], int x, int y, uint16_t lk, bool inner_row, bool live,
+                                         const StepParams &p)
+{
+    if (live) {
+        if (!inner_row || !interior_fluid(x, y, lk, p)) vec_edge_gather<PREC>(f, x, y, lk, p);
+        const MomentsF m = collide<PREC>(f, p);
+        if (p.write_results || x == p.W - 2) vec_write_observables<PREC>(m, x, y, p);
+    } else {
+#pragma unroll
+        for (int d = 0; d < 9; ++d) f[d] = 0.0f;
+    }
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(32 * VEC_ROWS, 4) k_nptl_vec(StepParams p)
+{
+    static_assert(PREC == F16S || PREC == BF16S, "2-byte shifted storage only");
+    const int lane = threadIdx.x;                              // blockDim.x == 32: a warp is a row segment
+    const int y = blockIdx.y * VEC_ROWS + threadIdx.y;
+    if (y >= p.H) return;                                      // uniform over the warp
+    const int xv = (blockIdx.x * 32 + lane) * VEC;
+    const bool vec_ok = xv < p.P;
+    const int x0 = vec_ok ? xv : p.P - VEC;                    // clamped: every lane loads inside the row
+    const unsigned short *S = static_cast<const unsigned short *>(p.lat0);
+    const size_t row0 = (size_t)y * p.P;
+    const bool inner_row = y > 0 && y < p.H - 1;
+
+    // r[d][k]: plane d's values for nodes x0 + 2k (low half) and x0 + 2k + 1 (high half)
+    unsigned r[9][4];
+    const uint4 l4 = *reinterpret_cast<const uint4 *>(p.links + row0 + x0);
+    if (inner_row) {
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {   // all nine loads are issued before any is used
+            const uint4 v = *reinterpret_cast<const uint4 *>(S + (size_t)d * p.N + (size_t)(y - cyd(d)) * p.P + x0);
+            r[d][0] = v.x; r[d][1] = v.y; r[d][2] = v.z; r[d][3] = v.w;
+        }
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {
+            const unsigned short *row = S + (size_t)d * p.N + (size_t)(y - cyd(d)) * p.P;
+            if (cxd(d) == 1) {            // source x - 1: shift up by one node, the previous lane's last node in front
+                unsigned prev = __shfl_up_sync(0xffffffffu, r[d][3] >> 16, 1);
+                if (lane == 0) prev = x0 >= 1 ? (unsigned)row[x0 - 1] : 0u;
+                r[d][3] = __byte_perm(r[d][2], r[d][3], 0x5432);
+                r[d][2] = __byte_perm(r[d][1], r[d][2], 0x5432);
+                r[d][1] = __byte_perm(r[d][0], r[d][1], 0x5432);
+                r[d][0] = __byte_perm(prev, r[d][0], 0x5410);
+            } else if (cxd(d) == -1) {    // source x + 1: shift down by one node, the next lane's first node behind
+                unsigned next = __shfl_down_sync(0xffffffffu, r[d][0] & 0xffffu, 1);
+                if (lane == 31) next = x0 + VEC < p.P ? (unsigned)row[x0 + VEC] : 0u;
+                r[d][0] = __byte_perm(r[d][0], r[d][1], 0x5432);
+                r[d][1] = __byte_perm(r[d][1], r[d][2], 0x5432);
+                r[d][2] = __byte_perm(r[d][2], r[d][3], 0x5432);
+                r[d][3] = __byte_perm(r[d][3], next, 0x5432);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int d = 0; d < 9; ++d) r[d][0] = r[d][1] = r[d][2] = r[d][3] = 0u;
+    }
+    const unsigned lw[4] = { l4.x, l4.y, l4.z, l4.w };
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {     // one pair of nodes at a time
+        float fa[9], fb[9];
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {
+            const float2 v = vec_unpack<PREC>(r[d][k]);
+            fa[d] = v.x;
+            fb[d] = v.y;
+        }
+        const int xa = x0 + 2 * k, xb = xa + 1;
+        const uint16_t la = (uint16_t)(lw[k] & 0xffffu), lb = (uint16_t)(lw[k] >> 16);
+        vec_node<PREC>(fa, xa, y, la, inner_row, vec_ok && xa < p.W && (la & LINK_FLUID), p);
+        vec_node<PREC>(fb, xb, y, lb, inner_row, vec_ok && xb < p.W && (lb & LINK_FLUID), p);
+#pragma unroll
+        for (int d = 0; d < 9; ++d) r[d][k] = vec_pack<PREC>(fa[d], fb[d]);
+    }
+    if (!vec_ok) return;
+    unsigned short *D = static_cast<unsigned short *>(p.lat1);
+#pragma unroll
+    for (int d = 0; d < 9; ++d)
+        *reinterpret_cast<uint4 *>(D + (size_t)d * p.N + row0 + x0) = make_uint4(r[d][0], r[d][1], r[d][2], r[d][3]);
 }
 
 // lptl: 1-D launch over n = x' + y' * P (padding columns x' >= W idle); each thread updates NY
@@ -177,7 +313,7 @@ __global__ void k_npol(StepParams p)
     __syncthreads();   // every read of this tile's old values happens before any write
     if (!fluid) return;
     if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
-    const Moments m = collide<PREC>(f, p);
+    const auto m = collide<PREC>(f, p);
 #pragma unroll
     for (int d = 0; d < 9; ++d) st<PREC>(p.lat0, lidx<L>(n, d, p.N), d, f[d], p);
     const int lx = threadIdx.x, ly = threadIdx.y;
@@ -229,7 +365,7 @@ __global__ void k_nsol_even(StepParams p)
         }
     }
     if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
-    const Moments m = collide<PREC>(f, p);
+    const auto m = collide<PREC>(f, p);
     if (fast) {
 #pragma unroll
         for (int d = 0; d < 9; ++d) st<PREC>(p.lat0, lidx<L>(n, d, p.N) - pull_delta<L>(d, p), d, f[d], p);
@@ -275,7 +411,7 @@ __global__ void k_nsol_odd(StepParams p)
         }
     }
     if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
-    const Moments m = collide<PREC>(f, p);
+    const auto m = collide<PREC>(f, p);
 #pragma unroll
     for (int d = 0; d < 9; ++d) st<PREC>(p.lat0, lidx<L>(n, 8 - d, p.N), 8 - d, f[d], p);
     observables<PREC>(m, xi, yi, p);

@@ -61,6 +61,21 @@ def test_q60_within_tolerance(plbm, oracle_mod, alg, lay):
     assert maxdiff(got, ref) <= 1e-12
 
 
+@pytest.mark.parametrize("precision", ["f16s", "bf16s"])
+@pytest.mark.parametrize("w,h,porous", [(203, 61, True), (300, 40, True), (62, 30, False), (520, 20, True)])
+def test_vectorised_rows_match_scalar_kernel(plbm, precision, w, h, porous):
+    """nptl/stream runs the 2-byte forms 8 nodes per thread with warp shuffles; lptl and the
+    collision layout run the scalar gather: same arithmetic, bit-identical results (row lengths
+    not a multiple of 8 or 256, porous obstacles, inlet, outlet, walls)."""
+    mask = plbm.porous_disks(w, h, 9, 0.7) if porous else None
+    scen = "Hagen-Poiseuille" if porous else "circle"
+    a = run_gpu(plbm, "nptl", "stream", scen, w, h, 300, precision=precision, mask=mask)
+    b = run_gpu(plbm, "lptl", "stream", scen, w, h, 300, precision=precision, mask=mask)
+    c = run_gpu(plbm, "nptl", "collision", scen, w, h, 300, precision=precision, mask=mask)
+    for k in a:
+        assert np.array_equal(a[k], b[k]) and np.array_equal(a[k], c[k]), k
+
+
 def test_q60_rejects_out_of_range_boundary(plbm):
     props = plbm.Properties("nptl", "stream", False, 64, 10, 10, "circle", 30, 62, 0.0, 0.0, 10.0, 0.0, 0.0, 1.0, 0.6)
     with pytest.raises(plbm.Exception, match="f64_q60"):
