@@ -268,13 +268,7 @@ int plbm_batch_create(unsigned n, const plbm_batch_domain *doms, int precision, 
         plbm::maxwell_boltzmann<double>(0, 0, s.outlet_density, d.feq_out);
         d.omega = 1 / s.relaxation_time;
         d.rho_out = s.outlet_density;
-        d.omegaf = (float)d.omega;
-        d.rho_outf = (float)(shifted ? d.rho_out - 1.0 : d.rho_out);
-        for (int k = 0; k < 9; ++k) {
-            d.weightf[k] = shifted ? 0.0f : (float)d.weight[k];
-            d.feq_inf[k] = (float)(shifted ? d.feq_in[k] - d.weight[k] : d.feq_in[k]);
-            d.feq_outf[k] = (float)(shifted ? d.feq_out[k] - d.weight[k] : d.feq_out[k]);
-        }
+        plbm::fill_float_constants(d, shifted, true, s.inlet_density, s.outlet_density);
         plbm::fill_q60_constants(d);
         // device buffers of the domain
         int8_t *flags = nullptr;
@@ -296,9 +290,11 @@ int plbm_batch_create(unsigned n, const plbm_batch_domain *doms, int precision, 
         e = cudaMemcpyAsync(flags, s.mask, (size_t)d.W * d.H, cudaMemcpyHostToDevice, b->stream);
         if (e == cudaSuccess) e = plbm::launch_links(flags, (uint16_t *)ptrs[2], d.W, d.H, d.P, b->stream);
         double rest[9];
-        for (int k = 0; k < 9; ++k) rest[k] = shifted ? 0.0 : d.weight[k];
-        if (e == cudaSuccess) e = plbm::launch_fill_lattice(ptrs[0], precision, plbm::STREAM, d.N, rest, b->stream);
-        if (e == cudaSuccess) e = plbm::launch_fill_lattice(ptrs[1], precision, plbm::STREAM, d.N, rest, b->stream);
+        for (int k = 0; k < 9; ++k) rest[k] = d.weight[k];
+        for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+            e = shifted ? plbm::launch_fill_shifted(ptrs[k], precision, plbm::STREAM, d.P, d.N, rest, d.shift_a, d.shift_g,
+                                                    b->stream)
+                        : plbm::launch_fill_lattice(ptrs[k], precision, plbm::STREAM, d.N, rest, b->stream);
         if (e == cudaSuccess) e = plbm::launch_fill_results(d.rho, d.jx, d.jy, d.jabs, (unsigned long long)d.W * d.H, b->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(jyc, 0, 2 * (size_t)d.H * 8, b->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);   // the mask buffer is the caller's

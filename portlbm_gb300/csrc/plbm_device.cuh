@@ -471,7 +471,8 @@ __device__ __forceinline__ void observables(const MomentsOf<PREC> &m, int xi, in
                             q_to_double(__double_as_longlong(m.jy)), q_to_double(__double_as_longlong(m.usq)) };
         write_observables(d, xi, yi, p);
     } else if constexpr (shifted<PREC>()) {
-        const Moments d = { 1.0 + (double)m.rho, (double)m.jx, (double)m.jy, (double)m.usq };   // rho = 1 + drho
+        // rho = rho0(x') + drho
+        const Moments d = { (p.shift_a - p.shift_g * xi) + (double)m.rho, (double)m.jx, (double)m.jy, (double)m.usq };
         write_observables(d, xi, yi, p);
     } else {
         write_observables(m, xi, yi, p);

@@ -574,15 +574,10 @@ struct plbm_handler {
             b.rho_out = (double)(float)props.orho;
         }
         const bool shifted = prec == PLBM_F32 || prec == PLBM_F16S || prec == PLBM_BF16S;
-        for (int d = 0; d < 9; ++d) {
-            // the shifted forms keep deviations from the rest state: ghosts are feq - w, rest is 0
-            b.weightf[d] = shifted ? 0.0f : (float)b.weight[d];
-            b.feq_inf[d] = shifted ? (float)(b.feq_in[d] - b.weight[d]) : (float)b.feq_in[d];
-            b.feq_outf[d] = shifted ? (float)(b.feq_out[d] - b.weight[d]) : (float)b.feq_out[d];
-        }
-        b.omegaf = (float)b.omega;
-        // outlet: f1+f4+f7+2(f8+f5+f2) carries exactly 1 in rest weights, so xv = (1 - rho_out) + sum(df)
-        b.rho_outf = shifted ? (float)(b.rho_out - 1.0) : (float)b.rho_out;
+        // the shifted forms keep deviations from w_d * rho0(x'): the straight inlet-outlet profile
+        // for the two-lattice pull schemes, rho0 = 1 for npol/nsol
+        b.W = W;
+        plbm::fill_float_constants(b, shifted, two_lattice(), props.irho, props.orho);
         {
             plbm::fill_q60_constants(b);
             b.status = status_d;
@@ -595,9 +590,14 @@ struct plbm_handler {
             }
         }
         double rest[9];
-        for (int d = 0; d < 9; ++d) rest[d] = shifted ? 0.0 : b.weight[d];
-        for (int i = 0; i < (two_lattice() ? 2 : 1); ++i)
-            cuda_check(plbm::launch_fill_lattice(lat[i], prec, lay, N, rest, stream), "lattice fill");
+        for (int d = 0; d < 9; ++d) rest[d] = b.weight[d];
+        for (int i = 0; i < (two_lattice() ? 2 : 1); ++i) {
+            if (shifted)   // rest state rho = 1: w_d (1 - rho0(x'))
+                cuda_check(plbm::launch_fill_shifted(lat[i], prec, lay, P, N, rest, b.shift_a, b.shift_g, stream),
+                           "lattice fill");
+            else
+                cuda_check(plbm::launch_fill_lattice(lat[i], prec, lay, N, rest, stream), "lattice fill");
+        }
 
         b.links = links;
         b.rho = res_d[0]; b.jx = res_d[1]; b.jy = res_d[2]; b.jabs = res_d[3];

@@ -29,11 +29,17 @@ __device__ __forceinline__ CT<PREC> pull_one(const void *S, unsigned long long n
 {
     const int sx = xi - cxd(d), sy = yi - cyd(d);
     if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H) {
-        if (sy < 0 || sy >= p.H) return g_weight<PREC>(p, d);
+        if (sy < 0 || sy >= p.H) {
+            if constexpr (shifted<PREC>()) return p.weightf[d] + p.shift_wg[d] * (float)xi;   // w_d (1 - rho0(x'))
+            else return g_weight<PREC>(p, d);
+        }
         return sx < 0 ? g_in<PREC>(p, d) : g_out<PREC>(p, d);
     }
     if (links & (1u << d)) return ld<PREC>(S, lidx<L>(n, 8 - d, p.N), 8 - d, p);
     const unsigned long long s = (unsigned long long)sx + (unsigned long long)sy * p.P;
+    if constexpr (shifted<PREC>()) {
+        if (cxd(d) != 0) return ld<PREC>(S, lidx<L>(s, d, p.N), d, p) + p.shift_cx[d];
+    }
     return ld<PREC>(S, lidx<L>(s, d, p.N), d, p);
 }
 
@@ -44,6 +50,14 @@ __device__ __forceinline__ long long pull_delta(int d, const StepParams &p)
 {
     const long long dn = -(long long)cxd(d) - (long long)cyd(d) * p.P;
     return L == COLLISION ? 9 * dn : (L == STREAM ? dn : 3 * dn);
+}
+
+// Shifted forms: values pulled from the neighbouring columns are re-referenced to this node's rho0.
+__device__ __forceinline__ void reference_shift(float f[9], const StepParams &p)
+{
+#pragma unroll
+    for (int d = 0; d < 9; ++d)
+        if (cxd(d) != 0) f[d] += p.shift_cx[d];
 }
 
 // Nodes away from the domain edge whose eight sources are all fluid take no per-direction checks.
@@ -73,6 +87,7 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
         if (interior_fluid(xi[j], yi[j], lk[j], p)) {
 #pragma unroll
             for (int d = 0; d < 9; ++d) f[j][d] = ld<PREC>(p.lat0, lidx<L>(n[j], d, p.N) + pull_delta<L>(d, p), d, p);
+            if constexpr (shifted<PREC>()) reference_shift(f[j], p);
         } else if (lk[j] & LINK_FLUID) {
 #pragma unroll
             for (int d = 0; d < 9; ++d) f[j][d] = pull_one<PREC, L>(p.lat0, n[j], xi[j], yi[j], d, lk[j], p);
@@ -116,15 +131,17 @@ constexpr int VEC_ROWS = 4;   // rows (warps) per block
 
 // Two packed 2-byte values <-> two floats with one conversion instruction each way; the same
 // values and round-to-nearest-even results as ld<PREC> / st<PREC>.
-template <int PREC> __device__ __forceinline__ float2 vec_unpack(unsigned w)
+// `shift` re-references the two values to the reading node's rho0 (shift_cx of the plane).
+template <int PREC> __device__ __forceinline__ float2 vec_unpack(unsigned w, float shift)
 {
     if constexpr (PREC == F16S) {
         __half2 h = *reinterpret_cast<__half2 *>(&w);
         const float2 v = __half22float2(h);
-        return make_float2(v.x * F16_UNSCALE, v.y * F16_UNSCALE);
+        return make_float2(fmaf(v.x, F16_UNSCALE, shift), fmaf(v.y, F16_UNSCALE, shift));
     } else {
         __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&w);
-        return __bfloat1622float2(h);
+        const float2 v = __bfloat1622float2(h);
+        return make_float2(v.x + shift, v.y + shift);
     }
 }
 template <int PREC> __device__ __forceinline__ unsigned vec_pack(float lo, float hi)
@@ -222,7 +239,9 @@ __global__ void __launch_bounds__(32 * VEC_ROWS, 4) k_nptl_vec(StepParams p)
         float fa[9], fb[9];
 #pragma unroll
         for (int d = 0; d < 9; ++d) {
-            const float2 v = vec_unpack<PREC>(r[d][k]);
+            // interior nodes take the re-referenced values; edge nodes re-gather them below
+            // (-0.0f leaves the x-resting planes exactly as the scalar gather reads them)
+            const float2 v = vec_unpack<PREC>(r[d][k], cxd(d) != 0 ? p.shift_cx[d] : -0.0f);
             fa[d] = v.x;
             fb[d] = v.y;
         }

@@ -16,6 +16,8 @@ cudaError_t launch_nsol(int prec, int lay, const StepParams &p, unsigned t, dim3
 // Set-up kernels (plbm_util.cu).
 cudaError_t launch_links(const int8_t *flags, uint16_t *links, int W, int H, int P, cudaStream_t s);
 cudaError_t launch_fill_lattice(void *lat, int prec, int lay, unsigned long long N, const double w[9], cudaStream_t s);
+cudaError_t launch_fill_shifted(void *lat, int prec, int lay, int P, unsigned long long N, const double w[9], double a,
+                                double g, cudaStream_t s);
 cudaError_t launch_fill_halo(void *halo, int prec, int W, int H, int ncb, int nrb, const double w[9], cudaStream_t s);
 cudaError_t launch_fill_results(double *rho, double *jx, double *jy, double *ja, unsigned long long n, cudaStream_t s);
 // FP64 sums over fluid nodes of the result arrays: out3 = {sum rho, sum jx, sum jy}.

@@ -33,6 +33,14 @@ struct StepParams {
     // would run on the FP64 pipe)
     float feq_inf[9], feq_outf[9], weightf[9];
     float omegaf, rho_outf;
+    // Shifted forms (F32, F16S, BF16S) hold f_d - w_d * rho0(x') with rho0(x') = shift_a - shift_g * x'.
+    // Two-lattice pull schemes use the straight profile between the inlet ghost column (x' = -1,
+    // rho_in) and the outlet ghost column (x' = W, rho_out); the others use rho0 = 1.  Every
+    // constant above is then relative to the rho0 of the node that reads it; a value pulled from
+    // column x' - cx_d is re-referenced by adding shift_cx[d] = w_d * shift_g * cx_d, and a wall
+    // ghost (rest state, rho = 1) reads weightf[d] + shift_wg[d] * x' = w_d (1 - rho0(x')).
+    double shift_a, shift_g;
+    float shift_wg[9], shift_cx[9];
     // F64_Q60: 64-bit fixed-point constants (value * 2^60, rounded from the double constants) and
     // the device word that records a population leaving the fixed-point range
     long long q_weight[9], q_feq_in[9], q_feq_out[9];

@@ -68,6 +68,42 @@ cudaError_t launch_fill_lattice(void *lat, int prec, int lay, unsigned long long
     return cudaGetLastError();
 }
 
+// Shifted forms: the rest state (rho = 1, j = 0) as deviations from w_d * rho0(x'),
+// rho0(x') = a - g x', i.e. w_d ((1 - a) + g x').
+template <int PREC>
+__global__ void k_fill_shifted(void *lat, int lay, int P, unsigned long long N, W9 w, double a, double g)
+{
+    const unsigned long long total = 9ull * N;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        int d;
+        unsigned long long n;
+        if (lay == COLLISION) { d = (int)(i % 9); n = i / 9; }
+        else if (lay == STREAM) { d = (int)(i / N); n = i % N; }
+        else { const unsigned long long r = i % (3 * N); d = 3 * (int)(i / (3 * N)) + (int)(r % 3); n = r / 3; }
+        const int x = (int)(n % (unsigned long long)P);
+        const float v = (float)(w.w[d] * ((1.0 - a) + g * x));
+        if constexpr (PREC == F16S) static_cast<__half *>(lat)[i] = __float2half_rn(v * F16_SCALE);
+        else if constexpr (PREC == BF16S) static_cast<__nv_bfloat16 *>(lat)[i] = __float2bfloat16_rn(v);
+        else static_cast<float *>(lat)[i] = v;
+    }
+}
+
+cudaError_t launch_fill_shifted(void *lat, int prec, int lay, int P, unsigned long long N, const double w[9], double a,
+                                double g, cudaStream_t s)
+{
+    W9 ww;
+    for (int i = 0; i < 9; ++i) ww.w[i] = w[i];
+    const int grid = 152 * 8, block = 256;
+    switch (prec) {
+    case F32: k_fill_shifted<F32><<<grid, block, 0, s>>>(lat, lay, P, N, ww, a, g); break;
+    case F16S: k_fill_shifted<F16S><<<grid, block, 0, s>>>(lat, lay, P, N, ww, a, g); break;
+    case BF16S: k_fill_shifted<BF16S><<<grid, block, 0, s>>>(lat, lay, P, N, ww, a, g); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
 // Halo snapshot entries hold the rest state initially; the direction of each slot follows the
 // layout documented at k_npol.
 template <int PREC>
@@ -218,7 +254,7 @@ __global__ void k_set_equilibrium(void *lat, StepParams p, const double *rho, co
         const double f = w * (R + 3 * cu + 4.5 * cu * cu - 1.5 * usq);
         typename Store<PREC>::C v;
         if constexpr (PREC == F64_Q60) v = double_to_q(f);
-        else if constexpr (shifted<PREC>()) v = (float)(f - w);
+        else if constexpr (shifted<PREC>()) v = (float)(f - w * (p.shift_a - p.shift_g * x));
         else v = (typename Store<PREC>::C)f;
         st<PREC>(lat, lidx<L>(n, d, p.N), d, v, p);
     }
