@@ -268,7 +268,8 @@ int plbm_batch_create(unsigned n, const plbm_batch_domain *doms, int precision, 
         plbm::maxwell_boltzmann<double>(0, 0, s.outlet_density, d.feq_out);
         d.omega = 1 / s.relaxation_time;
         d.rho_out = s.outlet_density;
-        plbm::fill_float_constants(d, shifted, true, s.inlet_density, s.outlet_density);
+        plbm::fill_float_constants(d, shifted, true, s.inlet_density, s.outlet_density,
+                                   precision == PLBM_F16S ? (double)plbm::F16_SCALE : 1.0);
         plbm::fill_q60_constants(d);
         // device buffers of the domain
         int8_t *flags = nullptr;

@@ -60,7 +60,10 @@ inline void fill_q60_constants(StepParams &b)
 // (b.W, b.weight, b.feq_in, b.feq_out, b.rho_out, b.omega must be set).  For the shifted forms
 // the reference density is rho0(x') = a - g x' (see StepParams): profile = true gives the straight
 // inlet-outlet profile a = rho_in - g, g = (rho_in - rho_out) / (W + 1); otherwise rho0 = 1.
-inline void fill_float_constants(StepParams &b, bool shifted, bool profile, double rho_in, double rho_out)
+// `scale` multiplies the shifted constants (F16_SCALE for the FP16 form, which computes on
+// scaled values).
+inline void fill_float_constants(StepParams &b, bool shifted, bool profile, double rho_in, double rho_out,
+                                 double scale = 1.0)
 {
     const double g = shifted && profile ? (rho_in - rho_out) / (b.W + 1) : 0.0;
     const double a = shifted && profile ? rho_in - g : 1.0;
@@ -70,15 +73,15 @@ inline void fill_float_constants(StepParams &b, bool shifted, bool profile, doub
     for (int d = 0; d < 9; ++d) {
         const double w = b.weight[d];
         const int cx = d % 3 - 1;
-        b.weightf[d] = shifted ? (float)(w * (1.0 - a)) : (float)w;
-        b.feq_inf[d] = shifted ? (float)(b.feq_in[d] - w * r_in) : (float)b.feq_in[d];
-        b.feq_outf[d] = shifted ? (float)(b.feq_out[d] - w * r_out) : (float)b.feq_out[d];
-        b.shift_wg[d] = (float)(w * g);
-        b.shift_cx[d] = (float)(w * g * cx);
+        b.weightf[d] = shifted ? (float)(w * (1.0 - a) * scale) : (float)w;
+        b.feq_inf[d] = shifted ? (float)((b.feq_in[d] - w * r_in) * scale) : (float)b.feq_in[d];
+        b.feq_outf[d] = shifted ? (float)((b.feq_out[d] - w * r_out) * scale) : (float)b.feq_out[d];
+        b.shift_wg[d] = (float)(w * g * scale);
+        b.shift_cx[d] = (float)(w * g * cx * scale);
     }
     b.omegaf = (float)b.omega;
     // outlet: f1+f4+f7+2(f8+f5+f2) carries exactly 1 in rest weights, so xv = (rho0 - rho_out) + sum(df)
-    b.rho_outf = shifted ? (float)(b.rho_out - r_out) : (float)b.rho_out;
+    b.rho_outf = shifted ? (float)((b.rho_out - r_out) * scale) : (float)b.rho_out;
 }
 
 }  // namespace plbm

@@ -59,9 +59,6 @@ template <> struct Store<F64_Q60> { using T = long long; using C = long long; };
 // not with f itself.
 template <int PREC> __host__ __device__ constexpr bool shifted() { return PREC == F32 || PREC == F16S || PREC == BF16S; }
 
-// FP16 holds df * 2^12: deviations down to ~1.5e-8 stay in half's normal range (min normal 6.1e-5)
-// while the largest deviations of a stable run (|df| < 1) stay far below its maximum, 65504.
-constexpr float F16_SCALE = 4096.0f, F16_UNSCALE = 1.0f / 4096.0f;
 
 template <int PREC>
 __device__ __forceinline__ typename Store<PREC>::C ld(const void *base, unsigned long long i, int d, const StepParams &p)
@@ -69,7 +66,7 @@ __device__ __forceinline__ typename Store<PREC>::C ld(const void *base, unsigned
     using T = typename Store<PREC>::T;
     const T *b = static_cast<const T *>(base);
     (void)d; (void)p;
-    if constexpr (PREC == F16S) return __half2float(b[i]) * F16_UNSCALE;
+    if constexpr (PREC == F16S) return __half2float(b[i]);   // df * F16_SCALE, the FP16 form's compute value
     else if constexpr (PREC == BF16S) return __bfloat162float(b[i]);
     else return b[i];
 }
@@ -80,7 +77,7 @@ __device__ __forceinline__ void st(void *base, unsigned long long i, int d, type
     using T = typename Store<PREC>::T;
     T *b = static_cast<T *>(base);
     (void)d; (void)p;
-    if constexpr (PREC == F16S) b[i] = __float2half_rn(v * F16_SCALE);
+    if constexpr (PREC == F16S) b[i] = __float2half_rn(v);
     else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(v);
     else b[i] = v;
 }
@@ -222,26 +219,28 @@ __device__ __forceinline__ MomentsF collide_f32_ref(float f[9], float omega)
     return { rho, jx, jy, usq };
 }
 
-// FP32 arithmetic for the F32 / F16S / BF16S storage forms (same regrouping as F64_FAST).
-__device__ __forceinline__ MomentsF collide_f32(float f[9], float omega)
+// FP32 arithmetic for the F32 / F16S / BF16S storage forms (same regrouping as F64_FAST).  The
+// FP16 form collides df * F16_SCALE: the update is linear in f except for the two quadratic
+// terms, whose coefficients take qs = 1 / F16_SCALE (qs = 1 for the other forms).
+__device__ __forceinline__ MomentsF collide_f32(float f[9], float omega, float qs)
 {
     const float A = f[2] + f[5] + f[8], B = f[0] + f[3] + f[6];
     const float C = f[6] + f[7] + f[8], E = f[0] + f[1] + f[2];
     const float rho = (B + (f[1] + f[4] + f[7])) + A;
     const float jx = A - B, jy = C - E;
     const float usq = fmaf(jx, jx, jy * jy);
-    const float R = fmaf(-1.5f, usq, rho);
+    const float R = fmaf(-1.5f * qs, usq, rho);
     const float om1 = 1.0f - omega;
     const float ow9 = omega * (1.0f / 9), ow36 = omega * (1.0f / 36), ow49 = omega * (4.0f / 9);
     const float b9 = ow9 * R, b36 = ow36 * R;
     f[4] = fmaf(om1, f[4], ow49 * R);
-    { const float u = jx, sym = fmaf(4.5f * ow9 * u, u, b9), odd = 3.0f * ow9;
+    { const float u = jx, sym = fmaf(4.5f * ow9 * qs * u, u, b9), odd = 3.0f * ow9;
       f[5] = fmaf(odd, u, fmaf(om1, f[5], sym)); f[3] = fmaf(-odd, u, fmaf(om1, f[3], sym)); }
-    { const float u = jy, sym = fmaf(4.5f * ow9 * u, u, b9), odd = 3.0f * ow9;
+    { const float u = jy, sym = fmaf(4.5f * ow9 * qs * u, u, b9), odd = 3.0f * ow9;
       f[7] = fmaf(odd, u, fmaf(om1, f[7], sym)); f[1] = fmaf(-odd, u, fmaf(om1, f[1], sym)); }
-    { const float u = jx + jy, sym = fmaf(4.5f * ow36 * u, u, b36), odd = 3.0f * ow36;
+    { const float u = jx + jy, sym = fmaf(4.5f * ow36 * qs * u, u, b36), odd = 3.0f * ow36;
       f[8] = fmaf(odd, u, fmaf(om1, f[8], sym)); f[0] = fmaf(-odd, u, fmaf(om1, f[0], sym)); }
-    { const float u = jx - jy, sym = fmaf(4.5f * ow36 * u, u, b36), odd = 3.0f * ow36;
+    { const float u = jx - jy, sym = fmaf(4.5f * ow36 * qs * u, u, b36), odd = 3.0f * ow36;
       f[2] = fmaf(odd, u, fmaf(om1, f[2], sym)); f[6] = fmaf(-odd, u, fmaf(om1, f[6], sym)); }
     return { rho, jx, jy, usq };
 }
@@ -367,7 +366,7 @@ __device__ __forceinline__ MomentsOf<PREC> collide(typename Store<PREC>::C f[9],
     else if constexpr (PREC == F64_FAST) return collide_f64_fast(f, p.omega);
     else if constexpr (PREC == F32_REF) return collide_f32_ref(f, p.omegaf);
     else if constexpr (PREC == F64_Q60) return collide_q60(f, p);
-    else return collide_f32(f, p.omegaf);
+    else return collide_f32(f, p.omegaf, PREC == F16S ? 1.0f / F16_SCALE : 1.0f);
 }
 
 // Outlet populations 0, 3, 6 of a border node (X-2, y), y in [2, V-3], from its other pulled
@@ -406,7 +405,8 @@ __device__ __forceinline__ void outlet_fill(typename Store<PREC>::C f[9], double
     } else {
         using C = typename Store<PREC>::C;
         const C xv = -p.rho_outf + ((f[1] + f[4] + f[7]) + (C)2 * (f[8] + f[5] + f[2]));
-        const C hd = (C)0.5 * (f[1] - f[7]), x6 = xv * (C)(1.0 / 6), hy = (C)(0.5 * jyo);
+        const C hd = (C)0.5 * (f[1] - f[7]), x6 = xv * (C)(1.0 / 6),
+                hy = (C)(0.5 * jyo * (PREC == F16S ? (double)F16_SCALE : 1.0));
         const C g0 = f[8], g1 = f[5], g2 = f[2];
         f[0] = g0 - hd - x6 - hy;
         f[3] = g1 - (C)(2.0 / 3) * xv;
@@ -471,8 +471,10 @@ __device__ __forceinline__ void observables(const MomentsOf<PREC> &m, int xi, in
                             q_to_double(__double_as_longlong(m.jy)), q_to_double(__double_as_longlong(m.usq)) };
         write_observables(d, xi, yi, p);
     } else if constexpr (shifted<PREC>()) {
-        // rho = rho0(x') + drho
-        const Moments d = { (p.shift_a - p.shift_g * xi) + (double)m.rho, (double)m.jx, (double)m.jy, (double)m.usq };
+        // rho = rho0(x') + drho; the FP16 form's moments carry F16_SCALE
+        const double us = PREC == F16S ? 1.0 / F16_SCALE : 1.0;
+        const Moments d = { (p.shift_a - p.shift_g * xi) + (double)m.rho * us, (double)m.jx * us, (double)m.jy * us,
+                            (double)m.usq * us * us };
         write_observables(d, xi, yi, p);
     } else {
         write_observables(m, xi, yi, p);

@@ -577,7 +577,8 @@ struct plbm_handler {
         // the shifted forms keep deviations from w_d * rho0(x'): the straight inlet-outlet profile
         // for the two-lattice pull schemes, rho0 = 1 for npol/nsol
         b.W = W;
-        plbm::fill_float_constants(b, shifted, two_lattice(), props.irho, props.orho);
+        plbm::fill_float_constants(b, shifted, two_lattice(), props.irho, props.orho,
+                                   prec == PLBM_F16S ? (double)plbm::F16_SCALE : 1.0);
         {
             plbm::fill_q60_constants(b);
             b.status = status_d;

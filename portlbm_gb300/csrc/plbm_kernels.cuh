@@ -137,7 +137,7 @@ template <int PREC> __device__ __forceinline__ float2 vec_unpack(unsigned w, flo
     if constexpr (PREC == F16S) {
         __half2 h = *reinterpret_cast<__half2 *>(&w);
         const float2 v = __half22float2(h);
-        return make_float2(fmaf(v.x, F16_UNSCALE, shift), fmaf(v.y, F16_UNSCALE, shift));
+        return make_float2(v.x + shift, v.y + shift);
     } else {
         __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&w);
         const float2 v = __bfloat1622float2(h);
@@ -147,7 +147,7 @@ template <int PREC> __device__ __forceinline__ float2 vec_unpack(unsigned w, flo
 template <int PREC> __device__ __forceinline__ unsigned vec_pack(float lo, float hi)
 {
     if constexpr (PREC == F16S) {
-        __half2 h = __floats2half2_rn(lo * F16_SCALE, hi * F16_SCALE);
+        __half2 h = __floats2half2_rn(lo, hi);
         return *reinterpret_cast<unsigned *>(&h);
     } else {
         __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
@@ -178,7 +178,8 @@ __device__ __forceinline__ void vec_node(float f[9], int x, int y, uint16_t lk, 
                                          const StepParams &p)
 {
     if (live) {
-        if (!inner_row || !interior_fluid(x, y, lk, p)) vec_edge_gather<PREC>(f, x, y, lk, p);
+        // links carry LINK_EDGE on the domain's edge, so this is interior_fluid() in one compare
+        if (lk != LINK_FLUID) vec_edge_gather<PREC>(f, x, y, lk, p);
         const MomentsF m = collide<PREC>(f, p);
         if (p.write_results || x == p.W - 2) vec_write_observables<PREC>(m, x, y, p);
     } else {

@@ -9,6 +9,15 @@ enum Layout { COLLISION = 0, STREAM = 1, BUNDLE = 2 };
 enum Precision { F64_STRICT = 0, F64_FAST = 1, F32_REF = 2, F32 = 3, F16S = 4, BF16S = 5, F64_Q60 = 6 };
 
 constexpr uint16_t LINK_FLUID = 1u << 4;
+// Set by k_links on the nodes of the first and last inner row and column: with it, an interior
+// fluid node whose eight sources are fluid is exactly links == LINK_FLUID.
+constexpr uint16_t LINK_EDGE = 1u << 9;
+
+// FP16 storage holds df * 2^12: deviations down to ~1.5e-8 stay in half's normal range (min
+// normal 6.1e-5) while the largest deviations of a stable run (|df| < 1) stay far below its
+// maximum, 65504.  The FP16 form also computes on these scaled values (its constants are scaled
+// the same way), so loads and stores need no rescaling.
+constexpr float F16_SCALE = 4096.0f;
 
 // Nodes per thread of the two-lattice kernels (nptl rows, lptl grid strides), per precision.
 constexpr int rows_per_thread(int) { return 1; }

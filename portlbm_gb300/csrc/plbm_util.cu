@@ -5,8 +5,8 @@
 
 namespace plbm {
 
-// Packs, for every inner node, whether it is fluid (bit 4) and which pull sources n - c_d are
-// solid (bit d).  flags: W*H int8 (0 fluid, 1 solid), row-major; links: P*H uint16.
+// Packs, for every inner node, whether it is fluid (bit 4), which pull sources n - c_d are
+// solid (bit d) and whether it lies on the domain's edge (LINK_EDGE).  flags: W*H int8 (0 fluid, 1 solid), row-major; links: P*H uint16.
 __global__ void k_links(const int8_t *flags, uint16_t *links, int W, int H, int P)
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
@@ -21,6 +21,7 @@ __global__ void k_links(const int8_t *flags, uint16_t *links, int W, int H, int 
             if (flags[(size_t)sy * W + sx] == 1) v |= (uint16_t)(1u << d);
         }
     }
+    if (x == 0 || x == W - 1 || y == 0 || y == H - 1) v |= LINK_EDGE;
     links[(size_t)y * P + x] = v;
 }
 
@@ -254,6 +255,7 @@ __global__ void k_set_equilibrium(void *lat, StepParams p, const double *rho, co
         const double f = w * (R + 3 * cu + 4.5 * cu * cu - 1.5 * usq);
         typename Store<PREC>::C v;
         if constexpr (PREC == F64_Q60) v = double_to_q(f);
+        else if constexpr (PREC == F16S) v = (float)((f - w * (p.shift_a - p.shift_g * x)) * F16_SCALE);
         else if constexpr (shifted<PREC>()) v = (float)(f - w * (p.shift_a - p.shift_g * x));
         else v = (typename Store<PREC>::C)f;
         st<PREC>(lat, lidx<L>(n, d, p.N), d, v, p);
