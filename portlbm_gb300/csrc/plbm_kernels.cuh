@@ -52,6 +52,25 @@ __device__ __forceinline__ long long pull_delta(int d, const StepParams &p)
     return L == COLLISION ? 9 * dn : (L == STREAM ? dn : 3 * dn);
 }
 
+// The float forms write their observables through a separate (not inlined) function taking the
+// four moments by value, so its FP64 widening is never scheduled into the per-node path (GB300
+// issues FP64 at 1/64 of the FP32 rate); the other forms write inline.
+template <int PREC>
+__device__ __noinline__ void observables_out(MomentsF m, int x, int y, const StepParams &p)
+{
+    observables<PREC>(m, x, y, p);
+}
+
+template <int PREC>
+__device__ __forceinline__ void emit_observables(const MomentsOf<PREC> &m, int x, int y, const StepParams &p)
+{
+    if constexpr (sizeof(typename Store<PREC>::C) == 4) {
+        if (p.write_results || x == p.W - 2) observables_out<PREC>(m, x, y, p);
+    } else {
+        observables<PREC>(m, x, y, p);
+    }
+}
+
 // Shifted forms: values pulled from the neighbouring columns are re-referenced to this node's rho0.
 __device__ __forceinline__ void reference_shift(float f[9], const StepParams &p)
 {
@@ -100,7 +119,7 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
         const auto m = collide<PREC>(f[j], p);
 #pragma unroll
         for (int d = 0; d < 9; ++d) st<PREC>(p.lat1, lidx<L>(n[j], d, p.N), d, f[j][d], p);
-        observables<PREC>(m, xi[j], yi[j], p);
+        emit_observables<PREC>(m, xi[j], yi[j], p);
     }
 }
 
@@ -155,9 +174,7 @@ template <int PREC> __device__ __forceinline__ unsigned vec_pack(float lo, float
     }
 }
 
-// Writing the observables is a separate (not inlined) function taking the four moments by value,
-// so its FP64 widening is never scheduled into the interior path (GB300 issues FP64 at 1/64 of
-// the FP32 rate).
+// The scalar gather of a vector-kernel node that is not interior fluid (edges, obstacles, outlet).
 template <int PREC>
 __device__ __forceinline__ void vec_edge_gather(float *f, int x, int y, uint16_t lk, const StepParams &p)
 {
@@ -168,12 +185,6 @@ __device__ __forceinline__ void vec_edge_gather(float *f, int x, int y, uint16_t
 }
 
 template <int PREC>
-__device__ __noinline__ void vec_write_observables(MomentsF m, int x, int y, const StepParams &p)
-{
-    observables<PREC>(m, x, y, p);
-}
-
-template <int PREC>
 __device__ __forceinline__ void vec_node(float f[9], int x, int y, uint16_t lk, bool inner_row, bool live,
                                          const StepParams &p)
 {
@@ -181,7 +192,7 @@ __device__ __forceinline__ void vec_node(float f[9], int x, int y, uint16_t lk, 
         // links carry LINK_EDGE on the domain's edge, so this is interior_fluid() in one compare
         if (lk != LINK_FLUID) vec_edge_gather<PREC>(f, x, y, lk, p);
         const MomentsF m = collide<PREC>(f, p);
-        if (p.write_results || x == p.W - 2) vec_write_observables<PREC>(m, x, y, p);
+        emit_observables<PREC>(m, x, y, p);
     } else {
 #pragma unroll
         for (int d = 0; d < 9; ++d) f[d] = 0.0f;
@@ -345,7 +356,7 @@ __global__ void k_npol(StepParams p)
         for (int k = 0; k < 3; ++k) st<PREC>(p.halo_out, halo_row(p, tcy, xi, k), 6 + k, f[6 + k], p);
     if (ly == 0 && tcy > 0)
         for (int k = 0; k < 3; ++k) st<PREC>(p.halo_out, halo_row(p, tcy - 1, xi, 3 + k), k, f[k], p);
-    observables<PREC>(m, xi, yi, p);
+    emit_observables<PREC>(m, xi, yi, p);
 }
 
 // ---- nsol: in-place AA swap ---------------------------------------------------------------
@@ -398,7 +409,7 @@ __global__ void k_nsol_even(StepParams p)
             st<PREC>(p.lat0, lidx<L>(t, d, p.N), d, f[d], p);
         }
     }
-    observables<PREC>(m, xi, yi, p);
+    emit_observables<PREC>(m, xi, yi, p);
 }
 
 template <int PREC, int L>
@@ -434,7 +445,7 @@ __global__ void k_nsol_odd(StepParams p)
     const auto m = collide<PREC>(f, p);
 #pragma unroll
     for (int d = 0; d < 9; ++d) st<PREC>(p.lat0, lidx<L>(n, 8 - d, p.N), 8 - d, f[d], p);
-    observables<PREC>(m, xi, yi, p);
+    emit_observables<PREC>(m, xi, yi, p);
 }
 
 }  // namespace plbm
