@@ -58,9 +58,10 @@ def peaks() -> dict:
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             d = json.load(f)
-        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d.get("bf16_tflops", 1900.0)),
+                "source": "measured"}
     except Exception:
-        return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
 class ClockSampler:
@@ -249,10 +250,10 @@ def batch_domains(plbm, n=256, seed=2024):
     return doms
 
 
-def batch_study(plbm, steps=100, precisions=("f32", "f16s")):
-    """Aggregate MLUPS of 256 uneven domains: one persistent tile-queue launch per step replayed from a
+def batch_study(plbm, steps=100, precisions=("f32", "f16s"), n=256):
+    """Aggregate MLUPS of `n` uneven domains: one persistent tile-queue launch per step replayed from a
     CUDA graph (tiles autotuned) against one launch per domain per step."""
-    doms = batch_domains(plbm)
+    doms = batch_domains(plbm, n=n)
     out = {"domains": len(doms)}
     for prec in precisions:
         b = plbm.Batch(doms, precision=prec)
@@ -274,6 +275,59 @@ def batch_study(plbm, steps=100, precisions=("f32", "f16s")):
                      "hbm_gbs_persistent_graph": round(bpn * nodes / ms_graph / 1e6, 1)}
         b.close()
     return out
+
+
+def nn_bench(batch=16, size=256, reps=5):
+    """Times the warm-start operator's kernels (csrc/plbm_nn.cu): one training step (forward,
+    backward, Adam) on `batch` channels of size^2 and one inference of a single channel, with
+    the convolution FLOPs (2 * pixels * 9 * Cin * Cout per layer; backward = 2 x forward)."""
+    import numpy as np
+    import torch
+    from portlbm_gb300 import warmstart as ws
+    model = ws.NeuralOperator(0)
+    rng = np.random.default_rng(0)
+
+    def flops(n):
+        f, h = 0.0, size
+        for lvl in range(5):
+            for ci, co in ws.ENC[2 * lvl:2 * lvl + 2]:
+                f += 2.0 * n * (h >> lvl) ** 2 * 9 * ci * co
+        for k, lvl in enumerate((3, 2, 1, 0)):
+            for ci, co in ws.DEC[2 * k:2 * k + 2]:
+                f += 2.0 * n * (h >> lvl) ** 2 * 9 * ci * co
+        return f + 2.0 * n * h * h * 9 * ws.HEAD[0] * ws.HEAD[1]
+
+    masks = torch.from_numpy((rng.random((batch, size, size)) < 0.3).astype(np.int8)).cuda()
+    x = model.assemble(masks, [ws.features(size, 1.02, 1.0, 0.8)] * batch)
+    grad = torch.zeros((batch, size, size, 3), dtype=torch.bfloat16, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for it in range(reps + 2):
+        if it == 2:
+            torch.cuda.synchronize()
+            e0.record()
+        model.forward(x, batch, size, size)
+        model.zero_grad()
+        model.backward(grad)
+        model.adam(lr=0.0)
+    e1.record()
+    torch.cuda.synchronize()
+    train_ms = e0.elapsed_time(e1) / reps
+    x1 = x[:1].contiguous()
+    for it in range(reps + 2):
+        if it == 2:
+            torch.cuda.synchronize()
+            e0.record()
+        model.forward(x1, 1, size, size)
+    e1.record()
+    torch.cuda.synchronize()
+    infer_ms = e0.elapsed_time(e1) / reps
+    pk = peaks()
+    train_tf = 3 * flops(batch) / (train_ms * 1e-3) / 1e12
+    infer_tf = flops(1) / (infer_ms * 1e-3) / 1e12
+    return {"train_step_ms": round(train_ms, 3), "train_tflops": round(train_tf, 2),
+            "infer_ms": round(infer_ms, 3), "infer_tflops": round(infer_tf, 2),
+            "bf16_peak_tflops": pk["bf16_tflops"], "train_frac_of_bf16_peak": round(train_tf / pk["bf16_tflops"], 4),
+            "config": f"U-Net 32-128 channels, train batch {batch} x {size}^2, inference 1 x {size}^2"}
 
 
 def load_traffic(kind: str, nodes: int):
@@ -364,6 +418,9 @@ def main():
     ap.add_argument("--warmstart-train", type=int, default=2000)
     ap.add_argument("--warmstart-test", type=int, default=200)
     ap.add_argument("--warmstart-save", default=None, help="write the trained weights (.npz) here")
+    ap.add_argument("--batch-study-only", action="store_true", help="only the batching study")
+    ap.add_argument("--batch-domains", type=int, default=256)
+    ap.add_argument("--nn-bench", action="store_true", help="only the warm-start operator's kernel timings")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -374,6 +431,12 @@ def main():
     import portlbm_gb300 as plbm
     from portlbm_gb300 import build as b
     b.build()
+    if args.batch_study_only or args.nn_bench:
+        if rank == 0:
+            key, res = (("batch_study", batch_study(plbm, n=args.batch_domains)) if args.batch_study_only
+                        else ("nn_bench", nn_bench()))
+            print(json.dumps({key: res}), flush=True)
+        return
     if args.warmstart_study:
         if rank == 0:
             from portlbm_gb300 import warmstart
