@@ -125,8 +125,13 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
 
 // nptl: 2-D blocks (tile shape from the work-group size hint); each thread updates NY
 // consecutive rows of its column.
+// Launch bounds of the 2-D step kernel: the Q60 form runs 256-thread blocks and is limited by
+// memory latency, so it is held to 48 registers for a fifth resident block per SM.
+template <int PREC> struct NptlBounds { static constexpr int threads = 512, blocks = 1; };
+template <> struct NptlBounds<F64_Q60> { static constexpr int threads = 256, blocks = 5; };
+
 template <int PREC, int L>
-__global__ void k_nptl(StepParams p)
+__global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::blocks) k_nptl(StepParams p)
 {
     constexpr int NY = RowsPerThread<PREC>::value;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
