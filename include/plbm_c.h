@@ -147,6 +147,33 @@ int plbm_make_flags(const plbm_properties *props, int8_t *out);
 int plbm_run_steps(plbm_handler *h, unsigned n, double *ms_per_step);
 /* Copies the device results to the host arrays now (as a frame step would). */
 int plbm_sync_results(plbm_handler *h);
+
+/* ---- headless frame export (replaces the reference's GUI frames, include/lbm/gui/lbm_gui.hpp:
+ * 825-870; no counterpart API) ----------------------------------------------------------------
+ * plbm_set_frame_export: from the next plbm_start on, every frame step (frameUpdateInterval) and
+ * the last step write the selected results (bit i of `fields` = PLBM_DENSITY + i) as
+ * <directory>/frame_<iteration, 9 digits>_<rho|jx|jy|jabs>.npy, float64, shape (H, W), row-major
+ * over the inner domain.  NULL/empty directory or fields = 0 turns it off.  The directory is
+ * created.  plbm_write_npy writes any rows x cols double array in the same format. */
+int plbm_set_frame_export(plbm_handler *h, const char *directory, unsigned fields);
+int plbm_write_npy(const char *path, const double *data, unsigned rows, unsigned cols);
+
+/* ---- benchmark driver (src/lbm/benchmark/benchmark.cpp:30-383, main_gpu.cpp:160-174) --------
+ * plbm_benchmark_run runs the reference's benchmark phases on libplbm handlers: phase 0 sweeps
+ * algorithms x dataLayouts x work-group sizes (plus lptl with "auto") for 10 steps, phase 1 the
+ * same for timeSteps and keeps each algorithm's fastest layout and work-group size (mean
+ * initialisation + run time), phase 2 runs that setup on every phaseTwoScenarios entry.  Settings
+ * come from settings_path read with node-count offset -2 (as the reference does), the sweep from
+ * benchmark_path (NULL: <root>/settings/benchmark.json, root = the settings file's grandparent
+ * directory).  Results go to <output_root or root>/benchmarks/phase<N>/ with the reference's file
+ * names and JSON shape; every entry also lists "mlups" per run and, if hbm_gbs > 0,
+ * "hbmFraction" (algorithmic bytes / run time / hbm_gbs).  phases: bit N runs phase N (0: all).
+ * Unlike the reference it does not rewrite settings.json for each configuration.
+ * plbm_benchmark_work_group_sizes: the work-group sizes the sweep tests for a device maximum
+ * (Benchmark::get_work_group_sizes, benchmark.cpp:30-62). */
+int plbm_benchmark_run(const char *settings_path, const char *benchmark_path, const char *output_root,
+                       const plbm_options *opts, unsigned phases, double hbm_gbs);
+int plbm_benchmark_work_group_sizes(unsigned max_work_group_size, unsigned *out, unsigned capacity, unsigned *count);
 /* Kernel launches issued per step (for launch accounting). */
 int plbm_launches_per_step(plbm_handler *h, unsigned *n);
 /* Algorithmic HBM bytes per node update of the hot kernel (9 loads + 9 stores). */

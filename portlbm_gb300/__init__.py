@@ -27,7 +27,7 @@ __all__ = [
     "Properties", "create_handler", "AlgorithmHandler", "Exception", "PropertyArgumentException",
     "WaitException", "CudaException", "ParseException", "NoDeviceException", "PRECISIONS",
     "properties_to_json", "json_to_properties", "library_path", "load_library", "compute_domain", "make_flags",
-    "porous_disks", "Batch",
+    "porous_disks", "Batch", "write_npy", "benchmark_work_group_sizes", "run_benchmark",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -114,6 +114,12 @@ _SIGS = {
     "plbm_mass_momentum": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "plbm_compute_domain": (ctypes.c_int, [ctypes.POINTER(_CProps), ctypes.POINTER(ctypes.c_uint)]),
     "plbm_make_flags": (ctypes.c_int, [ctypes.POINTER(_CProps), ctypes.c_void_p]),
+    "plbm_set_frame_export": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_uint]),
+    "plbm_write_npy": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_uint]),
+    "plbm_benchmark_run": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_COpts),
+                                          ctypes.c_uint, ctypes.c_double]),
+    "plbm_benchmark_work_group_sizes": (ctypes.c_int, [ctypes.c_uint, ctypes.POINTER(ctypes.c_uint), ctypes.c_uint,
+                                                       ctypes.POINTER(ctypes.c_uint)]),
     "plbm_set_equilibrium": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "plbm_run_to_residual": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_uint, ctypes.c_uint,
                                             ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_double)]),
@@ -372,6 +378,18 @@ class AlgorithmHandler:
     def sync_results(self) -> None:
         self._call("plbm_sync_results")
 
+    FIELDS = ("rho", "jx", "jy", "jabs")
+
+    def set_frame_export(self, directory, fields=FIELDS) -> None:
+        """Headless frames: from the next start() on, every frame step and the last step write the
+        chosen results as <directory>/frame_<iteration>_<field>.npy (float64, H x W).  None turns
+        it off.  (Stands in for the reference's GUI, include/lbm/gui/lbm_gui.hpp.)"""
+        bits = 0
+        for f in fields or ():
+            bits |= 1 << self.FIELDS.index(f)
+        self._call("plbm_set_frame_export", None if directory is None else str(directory).encode(),
+                   bits if directory is not None else 0)
+
     def set_equilibrium(self, rho, jx, jy) -> None:
         """Replaces the state by the equilibrium populations of the inner fields (W*H each, row-major;
         solid entries ignored); nptl/lptl only, before stepping or after an even number of steps."""
@@ -482,6 +500,44 @@ class Batch:
         n, t = ctypes.c_ulonglong(), ctypes.c_uint()
         self._ok(self._lib.plbm_batch_info(self._h, ctypes.byref(n), ctypes.byref(t)))
         return n.value, t.value
+
+
+def write_npy(path, array) -> None:
+    """A 2-D float64 array as .npy through the library's own writer (the frame-export format)."""
+    a = np.ascontiguousarray(array, dtype=np.float64)
+    if a.ndim != 2:
+        raise ValueError("write_npy takes a 2-D array")
+    _check(load_library().plbm_write_npy(str(path).encode(), a.ctypes.data, a.shape[0], a.shape[1]))
+
+
+def benchmark_work_group_sizes(max_work_group_size: int = 1024) -> list:
+    """The work-group sizes the benchmark sweep tests (Benchmark::get_work_group_sizes)."""
+    lib = load_library()
+    n = ctypes.c_uint()
+    lib.plbm_benchmark_work_group_sizes(max_work_group_size, None, 0, ctypes.byref(n))
+    out = (ctypes.c_uint * n.value)()
+    lib.plbm_benchmark_work_group_sizes(max_work_group_size, out, n.value, ctypes.byref(n))
+    return list(out)
+
+
+def run_benchmark(settings_path, benchmark_path=None, output_root=None, precision: str = "f64_strict",
+                  phases=(0, 1, 2), hbm_gbs: float = 0.0, device: int = 0) -> None:
+    """The reference's benchmark driver (src/lbm/benchmark/benchmark.cpp) on this library; see
+    plbm_benchmark_run in include/plbm_c.h.  Output under <output_root>/benchmarks/phase<N>/."""
+    lib = load_library()
+    opts = _COpts()
+    lib.plbm_default_options(ctypes.byref(opts))
+    opts.precision = PRECISIONS[precision]
+    opts.device = int(device)
+    mask = 0
+    for ph in phases:
+        mask |= 1 << int(ph)
+    rc = lib.plbm_benchmark_run(str(settings_path).encode(),
+                                None if benchmark_path is None else str(benchmark_path).encode(),
+                                None if output_root is None else str(output_root).encode(),
+                                ctypes.byref(opts), mask, float(hbm_gbs))
+    if rc != 0:
+        raise _CODES.get(rc, Exception)(f"benchmark failed ({rc})")
 
 
 def create_handler(source, precision: str = "f64_strict", mask=None, nan_protection: bool = True,

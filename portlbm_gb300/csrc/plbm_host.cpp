@@ -15,6 +15,7 @@
 #include "plbm_consts.h"
 #include "plbm_json.hpp"
 #include "plbm_launch.h"
+#include "plbm_power.h"
 
 #include <algorithm>
 #include <atomic>
@@ -23,6 +24,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <filesystem>
 #include <fstream>
 #include <memory>
 #include <mutex>
@@ -133,6 +135,34 @@ std::string read_file(const std::string &path)
     return ss.str();
 }
 
+// A rows x cols float64 array as a NumPy .npy file (format 1.0, little-endian, C order): the
+// headless stand-in for the reference's GUI frames.
+bool write_npy(const std::string &path, const double *data, unsigned rows, unsigned cols)
+{
+    std::string hdr = "{'descr': '<f8', 'fortran_order': False, 'shape': (" + std::to_string(rows) + ", " +
+                      std::to_string(cols) + "), }";
+    const size_t pre = 10;   // magic (6) + version (2) + header length (2)
+    size_t total = pre + hdr.size() + 1;
+    hdr.append((64 - total % 64) % 64, ' ');
+    hdr += '\n';
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return false;
+    const unsigned char magic[8] = { 0x93, 'N', 'U', 'M', 'P', 'Y', 1, 0 };
+    f.write(reinterpret_cast<const char *>(magic), 8);
+    const unsigned short hl = (unsigned short)hdr.size();
+    const unsigned char hlb[2] = { (unsigned char)(hl & 0xff), (unsigned char)(hl >> 8) };
+    f.write(reinterpret_cast<const char *>(hlb), 2);
+    f.write(hdr.data(), (std::streamsize)hdr.size());
+    for (size_t i = 0; i < (size_t)rows * cols; ++i) {   // explicit little-endian bytes
+        uint64_t u;
+        std::memcpy(&u, &data[i], 8);
+        unsigned char b[8];
+        for (int k = 0; k < 8; ++k) b[k] = (unsigned char)(u >> (8 * k));
+        f.write(reinterpret_cast<const char *>(b), 8);
+    }
+    return (bool)f;
+}
+
 struct JsonExtras {
     int precision = -1;
     int nan_protection = -1;
@@ -224,21 +254,8 @@ struct Domain {
         subdomain_horizontal_nodes, subdomain_count_vertical, subdomain_count_horizontal;
 };
 
-size_t which_power_of_4(size_t x)
-{
-    size_t checkbit = 3, pow = 0;
-    if ((x & 0x1) || x == 0) return 0;
-    while (!(checkbit & x)) { x >>= 2; pow++; }
-    return !(x & 2) ? pow : 0;
-}
-
-size_t which_power_of_2(size_t x)
-{
-    size_t checkbit = 1, pow = 0;
-    if ((x & 0x1) || x == 0) return 0;
-    while (!(checkbit & x)) { x >>= 1; pow++; }
-    return !(x >> 1 | 0) ? pow : 0;
-}
+using plbm::which_power_of_4;
+using plbm::which_power_of_2;
 
 void power_of_two_handling(size_t wg, unsigned &sv, unsigned &sh)
 {
@@ -406,6 +423,8 @@ struct plbm_handler {
     int *status_d = nullptr;
     double *jprev_d = nullptr;   // 2 * W*H: j of the previous residual evaluation
     long long jprev_iter = -1;   // iteration at which jprev_d was taken (-1: none)
+    std::string export_dir;      // frame export (empty: off)
+    unsigned export_fields = 0;  // bit i: result i (PLBM_DENSITY ..)
     double *res_h[4] = { nullptr, nullptr, nullptr, nullptr };
     size_t nres = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -703,6 +722,19 @@ struct plbm_handler {
             fail(PLBM_ERR_NUMERIC, "a population left the f64_q60 range [-4, 4) (unstable run?); rerun with f64_strict");
     }
 
+    // Frame export: the results of iteration `it` as <dir>/frame_<it>_<field>.npy (H x W).
+    void export_frame(unsigned it)
+    {
+        static const char *names[4] = { "rho", "jx", "jy", "jabs" };
+        char num[16];
+        std::snprintf(num, sizeof num, "%09u", it);
+        for (int i = 0; i < 4; ++i) {
+            if (!(export_fields & (1u << i))) continue;
+            const std::string path = export_dir + "/frame_" + num + "_" + names[i] + ".npy";
+            if (!write_npy(path, res_h[i], (unsigned)H, (unsigned)W)) fail(PLBM_ERR_IO, "cannot write " + path);
+        }
+    }
+
     void copy_results()
     {
         for (int i = 0; i < 4; ++i)
@@ -735,6 +767,7 @@ struct plbm_handler {
                     copy_results();
                     check_status();
                     end = t + 1;
+                    if (export_fields) export_frame(end);
                 }
                 const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c0).count();
                 frametime = ms / (double)(end - t);
@@ -1112,6 +1145,31 @@ int plbm_set_equilibrium(plbm_handler *h, const double *rho, const double *jx, c
         cuda_check(cudaStreamSynchronize(h->stream), "equilibrium");
         h->jprev_iter = -1;
     });
+}
+
+int plbm_set_frame_export(plbm_handler *h, const char *directory, unsigned fields)
+{
+    return guarded(h, [&] {
+        if (h->worker.joinable()) fail(PLBM_ERR_ARGUMENT, "plbm_set_frame_export while the step loop runs");
+        if (!directory || !*directory || fields == 0) {
+            h->export_dir.clear();
+            h->export_fields = 0;
+            return;
+        }
+        if (fields > 15u) fail(PLBM_ERR_ARGUMENT, "fields: bits 0..3 (density, x/y momentum, |momentum|)");
+        std::error_code ec;
+        std::filesystem::create_directories(directory, ec);
+        if (ec || !std::filesystem::is_directory(directory))
+            fail(PLBM_ERR_IO, std::string("cannot create export directory ") + directory);
+        h->export_dir = directory;
+        h->export_fields = fields;
+    });
+}
+
+int plbm_write_npy(const char *path, const double *data, unsigned rows, unsigned cols)
+{
+    if (!path || (!data && rows != 0 && cols != 0)) return PLBM_ERR_ARGUMENT;
+    return write_npy(path, data, rows, cols) ? PLBM_OK : PLBM_ERR_IO;
 }
 
 int plbm_sync_results(plbm_handler *h)
