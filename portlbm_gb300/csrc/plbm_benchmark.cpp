@@ -112,14 +112,20 @@ class Bench {
         return true;
     }
 
+    static void push(Json &entry, const char *key, double v)
+    {
+        Json &a = entry.set(key);
+        a.type = Json::ARRAY;
+        a.arr.push_back(plbm::jnum(v, false));
+    }
+
     void record(Json &entry, double init_s, double run_s)
     {
-        entry.set("initializationTimes").arr.push_back(plbm::jnum(init_s, false));
-        entry.set("runtimes").arr.push_back(plbm::jnum(run_s, false));
+        push(entry, "initializationTimes", init_s);
+        push(entry, "runtimes", run_s);
         const double nodes = (double)p_.vertical_nodes * p_.horizontal_nodes * p_.time_steps;
-        entry.set("mlups").arr.push_back(plbm::jnum(nodes / run_s / 1e6, false));
-        if (hbm_ > 0)
-            entry.set("hbmFraction").arr.push_back(plbm::jnum(nodes * bytes_node_ / run_s / (hbm_ * 1e9), false));
+        push(entry, "mlups", nodes / run_s / 1e6);
+        if (hbm_ > 0) push(entry, "hbmFraction", nodes * bytes_node_ / run_s / (hbm_ * 1e9));
     }
 
     Json file_header(const std::string &algorithm) const
