@@ -292,6 +292,14 @@ int plbm_nn_adam(float *w, const float *g, float *m, float *v, void *w_bf16, lon
                  float eps, int t, void *stream);
 /* Network input [N,H,W,C] (C >= 4): channel 0 the int8 solid mask, channels 1..3 the per-sample
  * scalars features[3n..3n+2] as constant planes, further channels zero. */
+/* 1 when plbm_nn_conv_fwd runs the shape (input channels Cin, output channels Cout) on the
+ * tcgen05 tensor-core kernel: Cin a multiple of 32, Cout <= 128, W a multiple of 128 or a power of
+ * two below 128 with H a multiple of 128 / W.  plbm_nn_conv_dgrad uses it with the two channel
+ * counts exchanged; other shapes and the weight gradient run the mma.sync kernel. */
+int plbm_nn_conv_on_tensor_cores(int H, int W, int Cin, int Cout);
+/* Synchronises the device and reports whether a tensor-core convolution gave up on a wait (its
+ * output is then invalid); clears the flag. */
+int plbm_nn_status(int *failed);
 int plbm_nn_assemble(const int8_t *mask, const float *features, void *y, int N, int H, int W, int C, void *stream);
 
 /* Last error message for h (or of the last failed create when h is NULL). */

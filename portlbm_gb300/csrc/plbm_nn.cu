@@ -8,8 +8,15 @@
 #include "../../include/plbm_c.h"
 
 #include <cuda_bf16.h>
+#include <mutex>
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+// Tensor-core convolution (plbm_nn_tc.cu).
+bool plbm_nn_tc_supported(int H, int W, int Cin, int Cout);
+int plbm_nn_tc_conv(const void *x, const void *w, const float *bias, void *y, int N, int H, int W, int Cin, int Cout,
+                    int relu, cudaStream_t s);
+int plbm_nn_tc_flip(const void *w, void *wt, int Cin, int Cout, cudaStream_t s);
 
 namespace {
 
@@ -305,6 +312,8 @@ extern "C" {
 int plbm_nn_conv_fwd(const void *x, const void *w, const float *bias, void *y, int N, int H, int W, int Cin,
                      int Cout, int relu, void *stream)
 {
+    if (plbm_nn_tc_supported(H, W, Cin, Cout))
+        return plbm_nn_tc_conv(x, w, bias, y, N, H, W, Cin, Cout, relu, (cudaStream_t)stream);
     ConvArgs a{};
     a.x = (const __nv_bfloat16 *)x; a.w = (const __nv_bfloat16 *)w; a.bias = bias; a.y = (__nv_bfloat16 *)y;
     a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout; a.relu = relu;
@@ -314,6 +323,25 @@ int plbm_nn_conv_fwd(const void *x, const void *w, const float *bias, void *y, i
 
 int plbm_nn_conv_dgrad(const void *g, const void *w, void *gx, int N, int H, int W, int Cin, int Cout, void *stream)
 {
+    // gx = conv3x3(g, W') with W'[ci][tap][co] = W[co][8 - tap][ci]: the forward kernel on the
+    // tensor cores, with the re-laid-out weights in a buffer kept for the process
+    if (plbm_nn_tc_supported(H, W, Cout, Cin)) {
+        static std::mutex mu;
+        static void *wt = nullptr;
+        static size_t cap = 0;
+        const size_t need = (size_t)Cin * 9 * Cout * 2;
+        std::lock_guard<std::mutex> lock(mu);
+        if (need > cap) {
+            if (wt) cudaFree(wt);
+            wt = nullptr;
+            cap = 0;
+            if (cudaMalloc(&wt, need) != cudaSuccess) return PLBM_ERR_CUDA;
+            cap = need;
+        }
+        const int rc = plbm_nn_tc_flip(w, wt, Cin, Cout, (cudaStream_t)stream);
+        if (rc != PLBM_OK) return rc;
+        return plbm_nn_tc_conv(g, wt, nullptr, gx, N, H, W, Cout, Cin, 0, (cudaStream_t)stream);
+    }
     ConvArgs a{};
     a.g = (const __nv_bfloat16 *)g; a.w = (const __nv_bfloat16 *)w; a.y = (__nv_bfloat16 *)gx;
     a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout;

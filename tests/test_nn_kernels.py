@@ -69,6 +69,38 @@ def test_conv_forward_and_gradients(plbm, n, h, w, cin, cout):
     assert np.max(np.abs(_np(gb) - rgb)) <= 1e-2 * np.max(np.abs(rgb)) + 1e-2
 
 
+@pytest.mark.parametrize("n,h,w,cin,cout", [(2, 8, 256, 32, 32), (1, 16, 128, 128, 96), (3, 4, 64, 64, 48),
+                                           (2, 32, 16, 32, 16), (1, 16, 32, 96, 128)])
+def test_tensor_core_convolution(plbm, n, h, w, cin, cout):
+    """The tcgen05 path (TMA-staged implicit GEMM, TMEM accumulator) against the CPU oracle, for the
+    forward pass and, with the channel counts exchanged, the input gradient."""
+    import torch
+    lib = _lib(plbm)
+    lib.plbm_nn_conv_on_tensor_cores.argtypes = [ctypes.c_int] * 4
+    lib.plbm_nn_status.argtypes = [ctypes.POINTER(ctypes.c_int)]
+    assert lib.plbm_nn_conv_on_tensor_cores(h, w, cin, cout) == 1
+    rng = np.random.default_rng(7 * cin + cout)
+    x = nn_ref.bf16_round(rng.standard_normal((n, h, w, cin)))
+    wt = nn_ref.bf16_round(rng.standard_normal((cout, 9 * cin)) / np.sqrt(9 * cin))
+    b = rng.standard_normal(cout).astype(np.float32)
+    y = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
+    xd, wd, bd = _bf(x), _bf(wt), torch.tensor(b).cuda()
+    for relu in (0, 1):
+        assert lib.plbm_nn_conv_fwd(xd.data_ptr(), wd.data_ptr(), bd.data_ptr(), y.data_ptr(), n, h, w, cin, cout,
+                                    relu, None) == 0
+        torch.cuda.synchronize()
+        _close(_np(y), nn_ref.conv_fwd(x, wt, b.astype(np.float64), bool(relu)))
+    if cin <= 128 and cout % 32 == 0:
+        assert lib.plbm_nn_conv_on_tensor_cores(h, w, cout, cin) == 1
+        g = nn_ref.bf16_round(rng.standard_normal((n, h, w, cout)))
+        gx = torch.empty((n, h, w, cin), dtype=torch.bfloat16, device="cuda")
+        assert lib.plbm_nn_conv_dgrad(_bf(g).data_ptr(), wd.data_ptr(), gx.data_ptr(), n, h, w, cin, cout, None) == 0
+        torch.cuda.synchronize()
+        _close(_np(gx), nn_ref.conv_dgrad(g, wt, cin))
+    failed = ctypes.c_int(-1)
+    assert lib.plbm_nn_status(ctypes.byref(failed)) == 0 and failed.value == 0
+
+
 def test_pool_and_upsample(plbm):
     import torch
     lib = _lib(plbm)
