@@ -31,8 +31,7 @@ constexpr int TC_KB = 32;           // channels per K block (64-byte rows)
 constexpr int TC_STAGES = 4;
 constexpr int TC_A_BYTES = TC_BM * TC_KB * 2;        // 8 KB
 constexpr int TC_B_MAX = 128 * TC_KB * 2;            // 8 KB at Npad = 128
-constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_MAX;
-constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /* alignment */ + 256 /* barriers */;
+constexpr int TC_SMEM = TC_STAGES * (TC_A_BYTES + TC_B_MAX) + 1024 /* alignment */ + 256 /* barriers */;   // largest
 constexpr long long TC_WAIT_CYCLES = 2000000000ll;   // ~1 s at the maximum SM clock
 
 __device__ int g_tc_error;
@@ -106,16 +105,17 @@ struct TcArgs {
     const float *bias;      // may be null
     int N, H, W, Cin, Cout, npad, relu;
     int BW, BH, tiles_x, tiles_y;
+    int stage_bytes;        // A tile + the B tile rounded up to 1024 B
     int *err;
 };
 
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, 4)
 k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap wmap, TcArgs a)
 {
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     // stages aligned to 1024 B (the swizzle pattern repeats every 512 B)
     unsigned char *smem = tc_smem_raw + ((1024 - (smem_u32(tc_smem_raw) & 1023)) & 1023);
-    unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + TC_STAGES * TC_STAGE_BYTES);
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + TC_STAGES * a.stage_bytes);
     unsigned long long *full = bars, *empty = bars + TC_STAGES, *done = bars + 2 * TC_STAGES;
     unsigned *tmem_slot = reinterpret_cast<unsigned *>(bars + 2 * TC_STAGES + 1);
     int *counts = reinterpret_cast<int *>(tmem_slot + 1);   // [0] issued, [1] consumed, [2] failed
@@ -155,7 +155,7 @@ k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUte
             }
             const int tap = it / kblocks, kb = it % kblocks;
             const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-            unsigned char *st = smem + s * TC_STAGE_BYTES;
+            unsigned char *st = smem + s * a.stage_bytes;
             const unsigned bar = smem_u32(&full[s]);
             mbar_expect_tx(bar, (unsigned)TC_A_BYTES + bbytes);
             tma_load_4d(smem_u32(st), &xmap, kb * TC_KB, x0 + dx, y0 + dy, n, bar);
@@ -172,7 +172,7 @@ k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUte
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const unsigned abase = smem_u32(smem + s * TC_STAGE_BYTES), bbase = abase + TC_A_BYTES;
+            const unsigned abase = smem_u32(smem + s * a.stage_bytes), bbase = abase + TC_A_BYTES;
 #pragma unroll
             for (int k = 0; k < TC_KB / 16; ++k)   // K = 16 per MMA: +32 B along the swizzled row
                 umma(tmem, smem_desc_sw64(abase + 32 * k), smem_desc_sw64(bbase + 32 * k), idesc, it > 0 || k > 0);
@@ -310,9 +310,11 @@ int plbm_nn_tc_conv(const void *x, const void *w, const float *bias, void *y, in
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return PLBM_ERR_ARGUMENT;
     }
-    TcArgs a{ (__nv_bfloat16 *)y, bias, N, H, W, Cin, Cout, npad, relu, BW, BH, W / BW, H / BH, err };
+    // stages sized by the padded output channels, so narrow layers fit more CTAs per SM
+    const int stage = TC_A_BYTES + (npad * TC_KB * 2 + 1023) / 1024 * 1024;
+    TcArgs a{ (__nv_bfloat16 *)y, bias, N, H, W, Cin, Cout, npad, relu, BW, BH, W / BW, H / BH, stage, err };
     const int tiles = N * a.tiles_x * a.tiles_y;
-    k_conv_tc<<<tiles, 128, TC_SMEM, s>>>(xmap, wmap, a);
+    k_conv_tc<<<tiles, 128, TC_STAGES * stage + 1024 + 256, s>>>(xmap, wmap, a);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
 }
 
