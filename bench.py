@@ -126,9 +126,12 @@ def make_props(plbm, alg, lay, w, h, steps, fui=None, wg=1024):
                            0.0, 1.0, 0.6)
 
 
-def device_run(plbm, precision, alg, lay, w, h, mask, steps, warmup):
+def device_run(plbm, precision, alg, lay, w, h, mask, steps, warmup, tau=None):
     """K device-resident steps; returns (ms_per_step, handler)."""
-    hd = plbm.create_handler(make_props(plbm, alg, lay, w, h, steps + warmup + 10), precision=precision, mask=mask)
+    props = make_props(plbm, alg, lay, w, h, steps + warmup + 10)
+    if tau is not None:
+        props.relaxation_time = float(tau)
+    hd = plbm.create_handler(props, precision=precision, mask=mask)
     hd.run_steps(warmup)
     ms = hd.run_steps(steps)
     return ms, hd
@@ -280,6 +283,28 @@ def batch_study(plbm, steps=100, precisions=("f32", "f16s"), n=256):
     return out
 
 
+def sweep(plbm, steps=50, warmup=5, sizes=((2000, 500), (8192, 8192)), taus=(0.55, 0.6, 1.0),
+          precisions=("f64_q60", "f64_strict")):
+    """The FP64 drop-in sweep: every algorithm x data layout on the circle channel (disk of radius
+    H/8 at W/4, walls, rho 1.2 / 1.0) at each size and relaxation time, device-resident steps timed
+    with CUDA events; MLUPS, algorithmic GB/s (144 B/node) and the fraction of measured HBM."""
+    pk = peaks()
+    rows = []
+    for w, h in sizes:
+        mask = circle_channel_mask(w, h)
+        for prec in precisions:
+            for tau in taus:
+                for alg in ("nptl", "lptl", "npol", "nsol"):
+                    for lay in ("stream", "collision", "bundle"):
+                        ms, hd = device_run(plbm, prec, alg, lay, w, h, mask, steps, warmup, tau)
+                        hd.close()
+                        gbs = BYTES_PER_NODE[prec] * w * h / (ms * 1e-3) / 1e9
+                        rows.append({"size": f"{w}x{h}", "precision": prec, "tau": tau, "algorithm": alg,
+                                     "data_layout": lay, "mlups": round(w * h / ms / 1e3, 1), "hbm_gbs": round(gbs, 1),
+                                     "frac_of_hbm": round(gbs / pk["hbm_gbs"], 4)})
+    return {"steps": steps, "peak_hbm_gbs": pk["hbm_gbs"], "rows": rows}
+
+
 def nn_bench(batch=16, size=256, reps=5):
     """Times the warm-start operator's kernels (csrc/plbm_nn.cu): one training step (forward,
     backward, Adam) on `batch` channels of size^2 and one inference of a single channel, with
@@ -424,6 +449,8 @@ def main():
     ap.add_argument("--batch-study-only", action="store_true", help="only the batching study")
     ap.add_argument("--batch-domains", type=int, default=256)
     ap.add_argument("--nn-bench", action="store_true", help="only the warm-start operator's kernel timings")
+    ap.add_argument("--sweep", action="store_true",
+                    help="only the FP64 sweep: 4 algorithms x 3 layouts x tau {0.55, 0.6, 1.0} at 2000x500 and 8192^2")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -434,10 +461,13 @@ def main():
     import portlbm_gb300 as plbm
     from portlbm_gb300 import build as b
     b.build()
-    if args.batch_study_only or args.nn_bench:
+    if args.batch_study_only or args.nn_bench or args.sweep:
         if rank == 0:
-            key, res = (("batch_study", batch_study(plbm, n=args.batch_domains)) if args.batch_study_only
-                        else ("nn_bench", nn_bench()))
+            if args.sweep:
+                key, res = "sweep", sweep(plbm)
+            else:
+                key, res = (("batch_study", batch_study(plbm, n=args.batch_domains)) if args.batch_study_only
+                            else ("nn_bench", nn_bench()))
             print(json.dumps({key: res}), flush=True)
         return
     if args.warmstart_study:
