@@ -26,6 +26,7 @@
 #include <cstring>
 #include <filesystem>
 #include <fstream>
+#include <future>
 #include <memory>
 #include <mutex>
 #include <sstream>
@@ -426,6 +427,24 @@ struct plbm_handler {
     std::string export_dir;      // frame export (empty: off)
     unsigned export_fields = 0;  // bit i: result i (PLBM_DENSITY ..)
     double *res_h[4] = { nullptr, nullptr, nullptr, nullptr };
+    // The pinned host result arrays are allocated and set to their initial values on a host
+    // thread while the device is already set up and stepping (pinning gigabytes takes a sizeable
+    // fraction of a second); every access waits for it first (wait_host()).
+    std::future<std::string> host_ready;
+    std::mutex host_mu;            // the step-loop thread and a caller's getter may both wait
+    std::string host_err;
+
+    std::string join_host()
+    {
+        std::lock_guard<std::mutex> g(host_mu);
+        if (host_ready.valid()) host_err = host_ready.get();
+        return host_err;
+    }
+    void wait_host()
+    {
+        const std::string err = join_host();
+        if (!err.empty()) fail(PLBM_ERR_CUDA, err);
+    }
     size_t nres = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
@@ -456,6 +475,8 @@ struct plbm_handler {
         for (auto &p : lat) { if (p) cudaFree(p); p = nullptr; }
         for (auto &p : halo) { if (p) cudaFree(p); p = nullptr; }
         for (auto &p : res_d) { if (p) cudaFree(p); p = nullptr; }
+        join_host();
+        host_err.clear();
         for (auto &p : res_h) { if (p) cudaFreeHost(p); p = nullptr; }
         if (links) cudaFree(links);
         if (flags_d) cudaFree(flags_d);
@@ -561,8 +582,15 @@ struct plbm_handler {
         cuda_check(cudaMalloc(&links, N * sizeof(uint16_t)), "cudaMalloc links");
         cuda_check(cudaMalloc(&flags_d, nres), "cudaMalloc flags");
         for (auto &r : res_d) cuda_check(cudaMalloc(&r, nres * sizeof(double)), "cudaMalloc results");
-        for (auto &r : res_h) cuda_check(cudaMallocHost(&r, nres * sizeof(double)), "cudaMallocHost results");
-        for (size_t i = 0; i < nres; ++i) { res_h[0][i] = -1.0; res_h[1][i] = 0; res_h[2][i] = 0; res_h[3][i] = 0; }
+        host_ready = std::async(std::launch::async, [this, dev = opt.device]() -> std::string {
+            if (cudaSetDevice(dev) != cudaSuccess) return "cudaSetDevice (host results)";
+            for (auto &r : res_h)
+                if (cudaMallocHost(&r, nres * sizeof(double)) != cudaSuccess) return "cudaMallocHost results";
+            // initial results: rho = -1, j = 0 (simulation.cpp:386-417)
+            std::fill(res_h[0], res_h[0] + nres, -1.0);
+            for (int i = 1; i < 4; ++i) std::fill(res_h[i], res_h[i] + nres, 0.0);
+            return std::string();
+        });
         cuda_check(cudaMalloc(&jy_d, 2ull * H * sizeof(double)), "cudaMalloc jy");
         cuda_check(cudaMemsetAsync(jy_d, 0, 2ull * H * sizeof(double), stream), "memset jy");
         cuda_check(cudaMalloc(&red_d, 3 * sizeof(double)), "cudaMalloc reduce");
@@ -725,6 +753,7 @@ struct plbm_handler {
     // Frame export: the results of iteration `it` as <dir>/frame_<it>_<field>.npy (H x W).
     void export_frame(unsigned it)
     {
+        wait_host();
         static const char *names[4] = { "rho", "jx", "jy", "jabs" };
         char num[16];
         std::snprintf(num, sizeof num, "%09u", it);
@@ -737,6 +766,7 @@ struct plbm_handler {
 
     void copy_results()
     {
+        wait_host();
         for (int i = 0; i < 4; ++i)
             cuda_check(cudaMemcpyAsync(res_h[i], res_d[i], nres * sizeof(double), cudaMemcpyDeviceToHost, stream),
                        "D2H results");
@@ -931,9 +961,11 @@ int plbm_is_finished(plbm_handler *h, int *finished)
 int plbm_get_results(plbm_handler *h, int which, const double **data, size_t *count)
 {
     if (which < 0 || which > 3) return set_err(h, Status{ PLBM_ERR_ARGUMENT, "which must be 0..3" });
-    *data = h->res_h[which];
-    *count = h->nres;
-    return PLBM_OK;
+    return guarded(h, [&] {
+        h->wait_host();
+        *data = h->res_h[which];
+        *count = h->nres;
+    });
 }
 
 int plbm_get_extents(plbm_handler *h, unsigned *hn, unsigned *vn)
