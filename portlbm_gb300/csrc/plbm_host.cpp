@@ -406,6 +406,7 @@ struct plbm_handler {
     plbm_options opt{};
     bool opt_precision_set = false;
     std::vector<int8_t> user_mask;
+    const int8_t *mask_src = nullptr;   // the caller's mask during plbm_create (uploaded from there)
     bool has_mask = false;
     Domain dom{};
     int alg = 0, lay = 0, prec = 0;
@@ -560,12 +561,12 @@ struct plbm_handler {
         outlet_mode = 0;
         if ((alg == 2 || alg == 3) && ((props.horizontal_nodes - 3) % dom.subdomain_horizontal_nodes) == 0) outlet_mode = 1;
 
-        if (has_mask) {
-            if (user_mask.size() != nres) fail(PLBM_ERR_ARGUMENT, "mask must hold inner W*H entries");
-            for (int8_t v : user_mask)
-                if (v != 0 && v != 1) fail(PLBM_ERR_ARGUMENT, "mask entries must be 0 (fluid) or 1 (solid)");
-        }
-        const std::vector<int8_t> flags = make_flags(props, has_mask ? &user_mask : nullptr);
+        if (has_mask && user_mask.size() != nres) fail(PLBM_ERR_ARGUMENT, "mask must hold inner W*H entries");
+        // a caller's mask is uploaded as it is (its 0/1 values are checked on the device below);
+        // otherwise the scenario's flags are built on the host
+        std::vector<int8_t> flags;
+        if (!has_mask) flags = make_flags(props, nullptr);
+        const int8_t *flags_src = has_mask ? (mask_src ? mask_src : user_mask.data()) : flags.data();
 
         cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
         cuda_check(cudaEventCreate(&ev0), "event");
@@ -596,7 +597,8 @@ struct plbm_handler {
         cuda_check(cudaMalloc(&red_d, 3 * sizeof(double)), "cudaMalloc reduce");
         cuda_check(cudaMalloc(&status_d, sizeof(int)), "cudaMalloc status");
         cuda_check(cudaMemsetAsync(status_d, 0, sizeof(int), stream), "memset status");
-        cuda_check(cudaMemcpyAsync(flags_d, flags.data(), nres, cudaMemcpyHostToDevice, stream), "H2D flags");
+        cuda_check(cudaMemcpyAsync(flags_d, flags_src, nres, cudaMemcpyHostToDevice, stream), "H2D flags");
+        if (has_mask) cuda_check(plbm::launch_check_mask(flags_d, nres, status_d, stream), "mask check");
         cuda_check(plbm::launch_links(flags_d, links, W, H, P, stream), "links kernel");
         cuda_check(plbm::launch_fill_results(res_d[0], res_d[1], res_d[2], res_d[3], nres, stream), "results fill");
 
@@ -687,6 +689,11 @@ struct plbm_handler {
             }
         }
         cuda_check(cudaStreamSynchronize(stream), "initialisation");
+        if (has_mask) {
+            int bad = 0;
+            cuda_check(cudaMemcpy(&bad, status_d, sizeof(int), cudaMemcpyDeviceToHost), "mask check");
+            if (bad) fail(PLBM_ERR_ARGUMENT, "mask entries must be 0 (fluid) or 1 (solid)");
+        }
     }
 
     cudaError_t launch_step(unsigned t, bool results)
@@ -875,11 +882,13 @@ static int create_common(plbm_handler *h, const plbm_options *opt, plbm_handler 
         if (h->opt.mask) {
             Props p = h->from_json ? json_to_props(h->settings_path, 0, nullptr) : h->props;
             const size_t n = (size_t)(p.horizontal_nodes - 2) * (p.vertical_nodes - 2);
-            h->user_mask.assign(h->opt.mask, h->opt.mask + n);
+            h->user_mask.assign(h->opt.mask, h->opt.mask + n);   // kept for initialize()
             h->has_mask = true;
+            h->mask_src = h->opt.mask;                             // valid during this call only
             h->opt.mask = nullptr;
         }
         h->build();
+        h->mask_src = nullptr;
     } catch (const Status &s) {
         set_err(nullptr, s);
         delete h;

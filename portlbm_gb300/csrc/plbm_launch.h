@@ -15,6 +15,7 @@ cudaError_t launch_nsol(int prec, int lay, const StepParams &p, unsigned t, dim3
 
 // Set-up kernels (plbm_util.cu).
 cudaError_t launch_links(const int8_t *flags, uint16_t *links, int W, int H, int P, cudaStream_t s);
+cudaError_t launch_check_mask(const int8_t *mask, unsigned long long n, int *bad, cudaStream_t s);
 cudaError_t launch_fill_lattice(void *lat, int prec, int lay, unsigned long long N, const double w[9], cudaStream_t s);
 cudaError_t launch_fill_shifted(void *lat, int prec, int lay, int P, unsigned long long N, const double w[9], double a,
                                 double g, cudaStream_t s);

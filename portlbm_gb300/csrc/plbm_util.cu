@@ -25,6 +25,22 @@ __global__ void k_links(const int8_t *flags, uint16_t *links, int W, int H, int 
     links[(size_t)y * P + x] = v;
 }
 
+// *bad = 1 if any entry of a caller's mask is neither 0 (fluid) nor 1 (solid).
+__global__ void k_check_mask(const int8_t *mask, unsigned long long n, int *bad)
+{
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        if (mask[i] != 0 && mask[i] != 1) { *bad = 1; return; }
+}
+
+cudaError_t launch_check_mask(const int8_t *mask, unsigned long long n, int *bad, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    k_check_mask<<<152 * 8, 256, 0, s>>>(mask, n, bad);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_links(const int8_t *flags, uint16_t *links, int W, int H, int P, cudaStream_t s)
 {
     dim3 grid((P + 255) / 256, H);
