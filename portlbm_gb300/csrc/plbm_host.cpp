@@ -780,37 +780,61 @@ struct plbm_handler {
         cuda_check(cudaStreamSynchronize(stream), "results copy");
     }
 
+    // Frame copies on the stream, without waiting (the host arrays are refreshed when the copy
+    // lands, as a reader of the reference's unsynchronised getters would observe).
+    void enqueue_results_copy()
+    {
+        wait_host();
+        for (int i = 0; i < 4; ++i)
+            cuda_check(cudaMemcpyAsync(res_h[i], res_d[i], nres * sizeof(double), cudaMemcpyDeviceToHost, stream),
+                       "D2H results");
+    }
+
     // The per-step loop of the drivers (nptl.hpp:121-139): stop when paused or finished; results
-    // go to the host on frame steps and after the final step.
+    // go to the host on frame steps and after the final step.  Steps and frame copies are
+    // enqueued without waiting; the host synchronises after about 5 ms of device work (at least
+    // 32 steps), at the end, on pause and before writing an exported frame, then checks the status
+    // word and publishes iteration, progress and the time per step.
     void loop()
     {
         try {
             cuda_check(cudaSetDevice(opt.device), "cudaSetDevice");
             const unsigned T = props.time_steps, F = props.frame_update_interval;
-            while (!stop.load() && iteration.load() < T) {
-                const unsigned t = iteration.load();
+            unsigned t = iteration.load(), done = t, max_pending = 32;
+            auto c0 = std::chrono::steady_clock::now();
+            auto publish = [&](unsigned upto) {
+                cuda_check(cudaStreamSynchronize(stream), "step");
+                check_status();
+                const auto c1 = std::chrono::steady_clock::now();
+                if (upto > done) frametime = std::chrono::duration<double, std::milli>(c1 - c0).count() / (double)(upto - done);
+                c0 = c1;
+                done = upto;
+                iteration = upto;
+                progress = (double)upto / (double)T;
+                const double per_step = frametime.load();
+                max_pending = per_step > 0 ? (unsigned)std::min(4096.0, std::max(32.0, 5.0 / per_step)) : 32u;
+            };
+            while (!stop.load() && t < T) {
                 unsigned frame = t + (F - 1 - t % F);
                 if (frame > T - 1) frame = T - 1;
-                const auto c0 = std::chrono::steady_clock::now();
                 unsigned end;
                 if (t < frame) {
                     const unsigned chunk = std::max<unsigned>(graph_steps ? graph_steps : 32, 32);
                     end = std::min(frame, t + chunk);
                     run_plain(t, end);
-                    cuda_check(cudaStreamSynchronize(stream), "step");
-                    check_status();
                 } else {
                     cuda_check(launch_step(t, true), "step");
-                    copy_results();
-                    check_status();
+                    enqueue_results_copy();
                     end = t + 1;
-                    if (export_fields) export_frame(end);
+                    if (export_fields) {
+                        publish(end);
+                        export_frame(end);
+                    }
                 }
-                const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c0).count();
-                frametime = ms / (double)(end - t);
-                iteration = end;
-                progress = (double)end / (double)T;
+                t = end;
+                if (t - done >= max_pending) publish(t);
             }
+            if (t != done) publish(t);
         } catch (const Status &s) {
             std::lock_guard<std::mutex> g(mu);
             worker_status = s.code;
