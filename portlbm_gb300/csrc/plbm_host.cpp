@@ -452,6 +452,8 @@ struct plbm_handler {
     plbm::StepParams base{};
     dim3 grid, block;
     cudaGraphExec_t gexec = nullptr;
+    cudaGraphExec_t frame_gexec[2] = { nullptr, nullptr };   // one frame, by starting parity
+    unsigned frame_graph_len = 0;
     unsigned graph_steps = 0;
 
     std::atomic<unsigned> iteration{ 0 };
@@ -473,6 +475,8 @@ struct plbm_handler {
         if (worker.joinable()) { stop = true; worker.join(); }
         if (gexec) cudaGraphExecDestroy(gexec);
         gexec = nullptr;
+        for (auto &f : frame_gexec) { if (f) cudaGraphExecDestroy(f); f = nullptr; }
+        frame_graph_len = 0;
         for (auto &p : lat) { if (p) cudaFree(p); p = nullptr; }
         for (auto &p : halo) { if (p) cudaFree(p); p = nullptr; }
         for (auto &p : res_d) { if (p) cudaFree(p); p = nullptr; }
@@ -731,6 +735,31 @@ struct plbm_handler {
         graph_steps = 2 * pairs;
     }
 
+    // One frame as a graph: F steps, the last writing the results, and the four result copies to
+    // the host; captured once per starting parity and replayed for every full frame.
+    cudaGraphExec_t frame_graph(unsigned t0, unsigned F)
+    {
+        const unsigned par = t0 & 1u;
+        if (frame_graph_len != F) {
+            for (auto &f : frame_gexec) { if (f) cudaGraphExecDestroy(f); f = nullptr; }
+            frame_graph_len = F;
+        }
+        if (frame_gexec[par]) return frame_gexec[par];
+        wait_host();   // the copies target the pinned host arrays
+        cudaGraph_t g = nullptr;
+        cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        cudaError_t e = cudaSuccess;
+        for (unsigned k = 0; k < F && e == cudaSuccess; ++k) e = launch_step(t0 + k, k + 1 == F);
+        for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+            e = cudaMemcpyAsync(res_h[i], res_d[i], nres * sizeof(double), cudaMemcpyDeviceToHost, stream);
+        cudaError_t e2 = cudaStreamEndCapture(stream, &g);
+        cuda_check(e, "frame capture");
+        cuda_check(e2, "end capture");
+        cuda_check(cudaGraphInstantiate(&frame_gexec[par], g, 0), "graph instantiate");
+        cudaGraphDestroy(g);
+        return frame_gexec[par];
+    }
+
     // Steps [t0, t1) with no result writes; graph replays where the parity allows.
     void run_plain(unsigned t0, unsigned t1)
     {
@@ -818,7 +847,11 @@ struct plbm_handler {
                 unsigned frame = t + (F - 1 - t % F);
                 if (frame > T - 1) frame = T - 1;
                 unsigned end;
-                if (t < frame) {
+                if (opt.use_graph && !export_fields && F >= 2 && F <= 256 && t % F == 0 && t + F <= T) {
+                    // a whole frame: one graph launch (steps, result writes and copies)
+                    cuda_check(cudaGraphLaunch(frame_graph(t, F), stream), "frame graph launch");
+                    end = t + F;
+                } else if (t < frame) {
                     const unsigned chunk = std::max<unsigned>(graph_steps ? graph_steps : 32, 32);
                     end = std::min(frame, t + chunk);
                     run_plain(t, end);
