@@ -700,11 +700,14 @@ struct plbm_handler {
         }
     }
 
-    cudaError_t launch_step(unsigned t, bool results)
+    // to_host: the step writes its observables straight into the pinned host arrays (device
+    // accessible on this platform) instead of the device arrays.
+    cudaError_t launch_step(unsigned t, bool results, bool to_host = false)
     {
         plbm::StepParams p = base;
         const unsigned par = t & 1u;
         p.write_results = results ? 1 : 0;
+        if (to_host) { p.rho = res_h[0]; p.jx = res_h[1]; p.jy = res_h[2]; p.jabs = res_h[3]; }
         p.lat0 = two_lattice() ? lat[par] : lat[0];
         p.lat1 = two_lattice() ? lat[par ^ 1u] : nullptr;
         p.jy_prev = jy_d + (size_t)par * H;
@@ -735,8 +738,9 @@ struct plbm_handler {
         graph_steps = 2 * pairs;
     }
 
-    // One frame as a graph: F steps, the last writing the results, and the four result copies to
-    // the host; captured once per starting parity and replayed for every full frame.
+    // One frame as a graph: F steps, the last writing its results straight into the pinned host
+    // arrays; captured once per starting parity and replayed for every full frame but the last
+    // (which also refreshes the device result arrays).
     cudaGraphExec_t frame_graph(unsigned t0, unsigned F)
     {
         const unsigned par = t0 & 1u;
@@ -749,9 +753,7 @@ struct plbm_handler {
         cudaGraph_t g = nullptr;
         cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         cudaError_t e = cudaSuccess;
-        for (unsigned k = 0; k < F && e == cudaSuccess; ++k) e = launch_step(t0 + k, k + 1 == F);
-        for (int i = 0; i < 4 && e == cudaSuccess; ++i)
-            e = cudaMemcpyAsync(res_h[i], res_d[i], nres * sizeof(double), cudaMemcpyDeviceToHost, stream);
+        for (unsigned k = 0; k < F && e == cudaSuccess; ++k) e = launch_step(t0 + k, k + 1 == F, k + 1 == F);
         cudaError_t e2 = cudaStreamEndCapture(stream, &g);
         cuda_check(e, "frame capture");
         cuda_check(e2, "end capture");
@@ -847,8 +849,8 @@ struct plbm_handler {
                 unsigned frame = t + (F - 1 - t % F);
                 if (frame > T - 1) frame = T - 1;
                 unsigned end;
-                if (opt.use_graph && !export_fields && F >= 2 && F <= 256 && t % F == 0 && t + F <= T) {
-                    // a whole frame: one graph launch (steps, result writes and copies)
+                if (opt.use_graph && !export_fields && F >= 2 && F <= 256 && t % F == 0 && t + F < T) {
+                    // a whole frame: one graph launch (its steps, results written to the host)
                     cuda_check(cudaGraphLaunch(frame_graph(t, F), stream), "frame graph launch");
                     end = t + F;
                 } else if (t < frame) {

@@ -150,6 +150,26 @@ def test_residual_decreases_and_steady_state_is_reached(plbm):
     assert np.all(np.isfinite(jx)) and jx[mask.reshape(-1) == 0].mean() > 0
 
 
+@pytest.mark.parametrize("frame", [10, 7])
+def test_frames_written_to_the_host_match_a_run_of_that_length(plbm, frame):
+    """Frames inside the step loop's frame graphs are written by the step kernel straight into the
+    host arrays: after a pause mid-run they equal a separate run of exactly that many steps."""
+    import time
+    props = plbm.Properties("nptl", "stream", False, 64, 10 ** 6, frame, "circle", 30, 62, 0.0, 0.0, 1.05, 0.0, 0.0,
+                            1.0, 0.6)
+    hd = plbm.create_handler(props, precision="f64_strict")
+    hd.start()
+    time.sleep(0.2)
+    hd.pause()
+    k = hd.get_current_iteration()
+    assert k > 0 and k % frame == 0
+    got = {"rho": hd.get_densities(), "jx": hd.get_x_velocities(), "jy": hd.get_y_velocities()}
+    hd.close()
+    ref = run_gpu(plbm, "nptl", "stream", "circle", 62, 30, k)
+    for key, v in got.items():
+        assert np.array_equal(v, ref[key]), key
+
+
 def test_residual_windows_chain_across_calls(plbm):
     """The snapshot of one call is the baseline of the next: K-step calls report the same residuals
     as one call over the same steps."""
