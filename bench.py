@@ -273,7 +273,8 @@ def batch_study(plbm, steps=100, precisions=("f32", "f16s"), n=256):
         ms_per = b.run(steps, mode="per_domain")
         bpn = BYTES_PER_NODE[prec]
         out[prec] = {"nodes": nodes, "tiles": tiles,
-                     "tile": {"threads": [tile[0], tile[1] & 255], "rows_per_thread": max(1, tile[1] >> 8),
+                     "tile": {"threads": [tile[0], tile[1] & 255], "rows_per_thread": max(1, (tile[1] >> 8) & 255),
+                              "vectorised_rows": bool(tile[1] & plbm.BATCH_TILE_VEC),
                               "blocks_per_sm": tile[2]},
                      "mlups_persistent_graph": round(nodes / ms_graph / 1e3, 1),
                      "mlups_persistent": round(nodes / ms_pers / 1e3, 1),

@@ -255,8 +255,12 @@ enum { PLBM_BATCH_PERSISTENT = 0, PLBM_BATCH_PERSISTENT_GRAPH = 1, PLBM_BATCH_PE
 int plbm_batch_create(unsigned n, const plbm_batch_domain *domains, int precision, plbm_batch **out);
 void plbm_batch_destroy(plbm_batch *b);
 /* Tile shape and resident blocks per SM of the persistent launch: a block of tile_w x (tile_h & 255)
- * threads, each sweeping (tile_h >> 8) rows (at least 1), so a tile covers
- * tile_w x ((tile_h & 255) * rows) nodes. */
+ * threads, each sweeping rows = ((tile_h >> 8) & 255) rows (at least 1), so a tile covers
+ * tile_w x ((tile_h & 255) * rows) nodes.  PLBM_BATCH_TILE_VEC in tile_h selects vectorised rows
+ * for PLBM_F16S / PLBM_BF16S batches (8 nodes per thread, one warp per 256-node row segment):
+ * tile_w must then be 32 and (tile_h & 255) at most 8, and a tile covers
+ * 256 x ((tile_h & 255) * rows) nodes. */
+#define PLBM_BATCH_TILE_VEC 0x10000
 int plbm_batch_set_tile(plbm_batch *b, int tile_w, int tile_h, int blocks_per_sm);
 /* Times `steps` persistent steps for each candidate tile shape and occupancy, keeps the fastest
  * (the timed steps advance the batch). */

@@ -429,6 +429,7 @@ class _CBatchDomain(ctypes.Structure):
 
 
 BATCH_MODES = {"persistent": 0, "persistent_graph": 1, "per_domain": 2}
+BATCH_TILE_VEC = 0x10000   # PLBM_BATCH_TILE_VEC: vectorised rows of the 2-byte batches (set_tile's tile_h)
 
 
 class Batch:
@@ -478,6 +479,7 @@ class Batch:
     __del__ = close
 
     def set_tile(self, tile_w: int, tile_h: int, blocks_per_sm: int = 8):
+        """tile_h = threads_y + 256 * rows per thread (+ BATCH_TILE_VEC for vectorised rows)."""
         self._ok(self._lib.plbm_batch_set_tile(self._h, tile_w, tile_h, blocks_per_sm))
 
     def autotune(self, steps: int = 4) -> tuple:

@@ -2,10 +2,10 @@
 // walks a queue of tiles drawn from every domain (atomic ticket counter, reset by a memset node),
 // and runs of steps are replayed from a captured CUDA graph.  Each domain keeps its own two
 // lattices (stream layout), links, geometry, relaxation time and boundary densities; the per-node
-// update is the nptl update of plbm_kernels.cuh (FP32 or FP16 shifted storage, or F64_Q60).
+// update is the nptl update of plbm_kernels.cuh (FP32, FP16 or BF16 shifted storage, or F64_Q60;
+// the 2-byte forms run the vectorised row update of k_nptl_vec, one warp per 256-node segment).
 //
-// There is no counterpart in the reference, which runs one domain per handler; this is the
-// "batching" addition of the GB300 build.
+// There is no counterpart in the reference, which runs one domain per handler.
 #include "../../include/plbm_c.h"
 #include "plbm_consts.h"
 #include "plbm_kernels.cuh"
@@ -42,29 +42,31 @@ __device__ __forceinline__ void stage_params(StepParams &dst, const StepParams &
 }
 
 // Persistent: every block takes tiles from the queue until it is empty; the tile's domain
-// parameters are staged in shared memory.
+// parameters are staged in shared memory.  The ticket of the next tile is claimed while the
+// current one is processed, so the queue's atomic is off the critical path.
 template <int PREC>
-__global__ void k_batch(BatchArgs a)
+__global__ void __launch_bounds__(256, PREC == F64_Q60 ? 3 : 6) k_batch(BatchArgs a)
 {
     __shared__ __align__(16) StepParams sp;
-    __shared__ unsigned s_tile, s_dom;
+    __shared__ unsigned s_tile;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     unsigned cur = 0xffffffffu;
+    if (tid == 0) s_tile = atomicAdd(a.ticket, 1u);
+    __syncthreads();
     for (;;) {
-        if (tid == 0) {
-            s_tile = atomicAdd(a.ticket, 1u);
-            s_dom = s_tile < a.n_tiles ? a.tile_domain[s_tile] : 0u;
-        }
-        __syncthreads();
-        const unsigned t = s_tile, dom = s_dom;
+        const unsigned t = s_tile;
         if (t >= a.n_tiles) return;
+        const unsigned dom = a.tile_domain[t];
+        __syncthreads();   // every thread has read s_tile
+        unsigned next = 0;
+        if (tid == 0) next = atomicAdd(a.ticket, 1u);
         if (dom != cur) {
             stage_params(sp, a.params[2 * dom + a.parity]);
             __syncthreads();
             if (tid == 0) sp.write_results = a.write_results;
+            __syncthreads();
             cur = dom;
         }
-        __syncthreads();
         const int local = (int)a.tile_local[t], txs = a.tiles_x[dom];
         const int xi = (local % txs) * a.tile_w + threadIdx.x;
         const int y0 = (local / txs) * a.tile_h * a.tile_rows + threadIdx.y;
@@ -72,14 +74,53 @@ __global__ void k_batch(BatchArgs a)
             const int yi = y0 + r * a.tile_h;
             if (xi < sp.W && yi < sp.H) {
                 const int xs[1] = { xi }, ys[1] = { yi };
-                update_two_lattice_rows<PREC, STREAM, 1>(xs, ys, sp);
+                update_two_lattice_rows<PREC, STREAM, 1, true>(xs, ys, sp);
             }
         }
-        __syncthreads();   // s_tile / s_dom are rewritten for the next tile
+        if (tid == 0) s_tile = next;
+        __syncthreads();   // sp and s_tile are rewritten for the next tile
     }
 }
 
-// One launch per domain (the comparison the batching form is measured against).
+// 2-byte storage: the same queue, each warp updating 256-node row segments with the vectorised
+// row update of k_nptl_vec (blockDim.x == 32; a tile is 256 x (tile_h * tile_rows) nodes).
+template <int PREC>
+__global__ void __launch_bounds__(256, 2) k_batch_vec(BatchArgs a)
+{
+    __shared__ __align__(16) StepParams sp;
+    __shared__ unsigned s_tile;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    unsigned cur = 0xffffffffu;
+    if (tid == 0) s_tile = atomicAdd(a.ticket, 1u);
+    __syncthreads();
+    for (;;) {
+        const unsigned t = s_tile;
+        if (t >= a.n_tiles) return;
+        const unsigned dom = a.tile_domain[t];
+        __syncthreads();
+        unsigned next = 0;
+        if (tid == 0) next = atomicAdd(a.ticket, 1u);
+        if (dom != cur) {
+            stage_params(sp, a.params[2 * dom + a.parity]);
+            __syncthreads();
+            if (tid == 0) sp.write_results = a.write_results;
+            __syncthreads();
+            cur = dom;
+        }
+        const int local = (int)a.tile_local[t], txs = a.tiles_x[dom];
+        const int xv = (local % txs) * (32 * VEC) + threadIdx.x * VEC;
+        const int y0 = (local / txs) * a.tile_h * a.tile_rows + threadIdx.y;
+        for (int r = 0; r < a.tile_rows; ++r) {
+            const int yi = y0 + r * a.tile_h;
+            if (yi < sp.H) vec_row_segment<PREC>(sp, yi, xv, threadIdx.x);   // uniform over the warp
+        }
+        if (tid == 0) s_tile = next;
+        __syncthreads();
+    }
+}
+
+// One launch per domain with the same per-node update (the comparison the batching form is
+// measured against).
 template <int PREC>
 __global__ void k_batch_single(BatchArgs a, unsigned domain)
 {
@@ -91,7 +132,7 @@ __global__ void k_batch_single(BatchArgs a, unsigned domain)
     const int xi = blockIdx.x * blockDim.x + threadIdx.x, yi = blockIdx.y * blockDim.y + threadIdx.y;
     if (xi < sp.W && yi < sp.H) {
         const int xs[1] = { xi }, ys[1] = { yi };
-        update_two_lattice_rows<PREC, STREAM, 1>(xs, ys, sp);
+        update_two_lattice_rows<PREC, STREAM, 1, true>(xs, ys, sp);
     }
 }
 
@@ -134,6 +175,11 @@ struct plbm_batch {
     }
 
     unsigned n_domains() const { return (unsigned)(host.size() / 2); }
+    bool two_byte() const { return prec == PLBM_F16S || prec == PLBM_BF16S; }
+    // vectorised rows (2-byte storage only): one warp per 256-node row segment
+    bool vec_rows = false;
+    bool vec() const { return vec_rows; }
+    int tile_nodes_w() const { return vec() ? 32 * plbm::VEC : tile_w; }
 
     // Tiles of every domain in domain order; the queue hands them out in that order.
     cudaError_t build_tiles()
@@ -142,7 +188,8 @@ struct plbm_batch {
         std::vector<int> tx;
         for (unsigned i = 0; i < n_domains(); ++i) {
             const StepParams &d = host[2 * i];
-            const int nx = (d.W + tile_w - 1) / tile_w, ny = (d.H + tile_h * tile_rows - 1) / (tile_h * tile_rows);
+            const int tw = tile_nodes_w();
+            const int nx = (d.W + tw - 1) / tw, ny = (d.H + tile_h * tile_rows - 1) / (tile_h * tile_rows);
             tx.push_back(nx);
             for (int k = 0; k < nx * ny; ++k) { dom.push_back(i); loc.push_back((unsigned)k); }
         }
@@ -174,8 +221,14 @@ struct plbm_batch {
         const dim3 block(tile_w, tile_h);
         switch (prec) {
         case PLBM_F32: plbm::k_batch<plbm::F32><<<blocks, block, 0, stream>>>(a); break;
-        case PLBM_F16S: plbm::k_batch<plbm::F16S><<<blocks, block, 0, stream>>>(a); break;
-        case PLBM_BF16S: plbm::k_batch<plbm::BF16S><<<blocks, block, 0, stream>>>(a); break;
+        case PLBM_F16S:
+            if (vec()) plbm::k_batch_vec<plbm::F16S><<<blocks, block, 0, stream>>>(a);
+            else plbm::k_batch<plbm::F16S><<<blocks, block, 0, stream>>>(a);
+            break;
+        case PLBM_BF16S:
+            if (vec()) plbm::k_batch_vec<plbm::BF16S><<<blocks, block, 0, stream>>>(a);
+            else plbm::k_batch<plbm::BF16S><<<blocks, block, 0, stream>>>(a);
+            break;
         default: plbm::k_batch<plbm::F64_Q60><<<blocks, block, 0, stream>>>(a); break;
         }
         return cudaGetLastError();
@@ -327,10 +380,15 @@ void plbm_batch_destroy(plbm_batch *b) { delete b; }
 
 int plbm_batch_set_tile(plbm_batch *b, int tile_w, int tile_h, int blocks_per_sm)
 {
-    // tile_h carries the rows each thread sweeps in its upper bits: tile_h = threads_y + 256 * rows
-    const int ty = tile_h & 255, rows = std::max(1, tile_h >> 8);
+    // tile_h carries the rows each thread sweeps and the vectorised-rows flag in its upper bits:
+    // tile_h = threads_y + 256 * rows (+ PLBM_BATCH_TILE_VEC)
+    const int ty = tile_h & 255, rows = std::max(1, (tile_h >> 8) & 255);
+    const bool v = (tile_h & PLBM_BATCH_TILE_VEC) != 0;
     if (tile_w < 1 || ty < 1 || tile_w * ty > 1024 || blocks_per_sm < 1)
         return berr(b, PLBM_ERR_ARGUMENT, "tile must have 1..1024 threads");
+    if (v && (!b->two_byte() || tile_w != 32 || ty > 8))
+        return berr(b, PLBM_ERR_ARGUMENT, "vectorised rows: PLBM_F16S / PLBM_BF16S batches, tiles of 32 x (1..8) threads");
+    b->vec_rows = v;
     b->tile_w = tile_w;
     b->tile_h = ty;
     b->tile_rows = rows;
@@ -381,16 +439,28 @@ int plbm_batch_autotune(plbm_batch *b, unsigned steps, int *tile_w, int *tile_h,
     // threads_x, threads_y + 256 * rows swept per thread
     static const int cand[][2] = { { 32, 4 + 256 * 1 }, { 32, 4 + 256 * 4 }, { 32, 4 + 256 * 8 }, { 32, 8 + 256 * 4 },
                                    { 64, 2 + 256 * 8 }, { 64, 4 + 256 * 4 }, { 128, 2 + 256 * 4 } };
+    // 2-byte batches also try vectorised rows (fast in open channels; porous domains send many
+    // nodes through the scalar edge gather and favour one node per thread)
+    static const int cand_vec[][2] = { { 32, 4 + 256 * 1 }, { 32, 4 + 256 * 2 }, { 32, 4 + 256 * 4 }, { 32, 8 + 256 * 1 },
+                                       { 32, 8 + 256 * 2 }, { 32, 2 + 256 * 4 }, { 32, 2 + 256 * 8 } };
     static const int bps[] = { 4, 8, 16 };
+    static const int bps_vec[] = { 2, 4, 8 };
     double best = 1e300;
-    int bw = b->tile_w, bh = b->tile_h + 256 * b->tile_rows, bb = 8;
+    int bw = b->tile_w, bh = b->tile_h + 256 * b->tile_rows + (b->vec_rows ? PLBM_BATCH_TILE_VEC : 0), bb = 8;
+    auto tryit = [&](int w, int h, int k) {
+        if (plbm_batch_set_tile(b, w, h, k) != PLBM_OK) return PLBM_OK;
+        double ms = 0;
+        if (plbm_batch_run(b, steps, PLBM_BATCH_PERSISTENT, &ms) != PLBM_OK) return PLBM_ERR_CUDA;
+        if (ms < best) { best = ms; bw = w; bh = h; bb = k; }
+        return PLBM_OK;
+    };
     for (const auto &c : cand)
-        for (int k : bps) {
-            if (plbm_batch_set_tile(b, c[0], c[1], k) != PLBM_OK) continue;
-            double ms = 0;
-            if (plbm_batch_run(b, steps, PLBM_BATCH_PERSISTENT, &ms) != PLBM_OK) return PLBM_ERR_CUDA;
-            if (ms < best) { best = ms; bw = c[0]; bh = c[1]; bb = k; }
-        }
+        for (int k : bps)
+            if (tryit(c[0], c[1], k) != PLBM_OK) return PLBM_ERR_CUDA;
+    if (b->two_byte())
+        for (const auto &c : cand_vec)
+            for (int k : bps_vec)
+                if (tryit(c[0], c[1] + PLBM_BATCH_TILE_VEC, k) != PLBM_OK) return PLBM_ERR_CUDA;
     const int rc = plbm_batch_set_tile(b, bw, bh, bb);
     if (tile_w) *tile_w = bw;
     if (tile_h) *tile_h = bh;   // threads_y + 256 * rows

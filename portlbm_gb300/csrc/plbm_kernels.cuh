@@ -71,14 +71,6 @@ __device__ __forceinline__ void emit_observables(const MomentsOf<PREC> &m, int x
     }
 }
 
-// Shifted forms: values pulled from the neighbouring columns are re-referenced to this node's rho0.
-__device__ __forceinline__ void reference_shift(float f[9], const StepParams &p)
-{
-#pragma unroll
-    for (int d = 0; d < 9; ++d)
-        if (cxd(d) != 0) f[d] += p.shift_cx[d];
-}
-
 // Nodes away from the domain edge whose eight sources are all fluid take no per-direction checks.
 __device__ __forceinline__ bool interior_fluid(int xi, int yi, uint16_t lk, const StepParams &p)
 {
@@ -89,9 +81,20 @@ __device__ __forceinline__ bool interior_fluid(int xi, int yi, uint16_t lk, cons
 // several nodes before computing any of them to keep enough bytes in flight per SM.
 template <int PREC> struct RowsPerThread { static constexpr int value = rows_per_thread(PREC); };
 
-template <int PREC, int L, int NY>
+// The gather of one node.  Away from the domain edge every source is the neighbour or, behind a
+// solid, the node's own opposite population (pull_one); edge nodes take pull_one.  Three forms,
+// chosen by measurement, give the same values:
+//  * unshifted storage: interior nodes without solid neighbours load plainly, nodes next to an
+//    obstacle select each source; no loaded value is used inside the branches, so a warp split
+//    between them waits for one round of loads;
+//  * shifted storage, POROUS: one selected load per direction for every interior node, the
+//    re-referencing shift added after the branches (domains full of obstacles);
+//  * shifted storage otherwise: plain loads and the shift for interior nodes without solid
+//    neighbours, pull_one for the rest (open channels).
+template <int PREC, int L, int NY, bool POROUS = false>
 __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const int yi[NY], const StepParams &p)
 {
+    constexpr bool SH = shifted<PREC>();
     CT<PREC> f[NY][9];
     uint16_t lk[NY];
     unsigned long long n[NY];
@@ -103,10 +106,21 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
     }
 #pragma unroll
     for (int j = 0; j < NY; ++j) {
-        if (interior_fluid(xi[j], yi[j], lk[j], p)) {
+        const bool interior = (lk[j] & (LINK_FLUID | LINK_EDGE)) == LINK_FLUID;
+        if ((!SH || !POROUS) && lk[j] == LINK_FLUID) {
 #pragma unroll
-            for (int d = 0; d < 9; ++d) f[j][d] = ld<PREC>(p.lat0, lidx<L>(n[j], d, p.N) + pull_delta<L>(d, p), d, p);
-            if constexpr (shifted<PREC>()) reference_shift(f[j], p);
+            for (int d = 0; d < 9; ++d) {
+                f[j][d] = ld<PREC>(p.lat0, lidx<L>(n[j], d, p.N) + pull_delta<L>(d, p), d, p);
+                if constexpr (SH && !POROUS)
+                    if (cxd(d) != 0) f[j][d] += p.shift_cx[d];
+            }
+        } else if ((!SH || POROUS) && interior) {
+#pragma unroll
+            for (int d = 0; d < 9; ++d) {
+                const bool bounce = d != 4 && ((lk[j] >> d) & 1u);
+                f[j][d] = ld<PREC>(p.lat0, bounce ? lidx<L>(n[j], 8 - d, p.N) : lidx<L>(n[j], d, p.N) + pull_delta<L>(d, p),
+                                   d, p);
+            }
         } else if (lk[j] & LINK_FLUID) {
 #pragma unroll
             for (int d = 0; d < 9; ++d) f[j][d] = pull_one<PREC, L>(p.lat0, n[j], xi[j], yi[j], d, lk[j], p);
@@ -115,6 +129,14 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
 #pragma unroll
     for (int j = 0; j < NY; ++j) {
         if (!(lk[j] & LINK_FLUID)) continue;
+        if constexpr (SH && POROUS) {
+            // values pulled from the neighbouring columns are re-referenced to this node's rho0
+            if (!(lk[j] & LINK_EDGE)) {
+#pragma unroll
+                for (int d = 0; d < 9; ++d)
+                    if (cxd(d) != 0 && !((lk[j] >> d) & 1u)) f[j][d] += p.shift_cx[d];
+            }
+        }
         if (is_outlet_row(xi[j], yi[j], p)) outlet_fill<PREC>(f[j], p.jy_prev[yi[j]], p);
         const auto m = collide<PREC>(f[j], p);
 #pragma unroll
@@ -204,14 +226,12 @@ __device__ __forceinline__ void vec_node(float f[9], int x, int y, uint16_t lk, 
     }
 }
 
+// One warp updates the row segment of row y whose lane `lane` owns nodes xv .. xv + VEC - 1
+// (xv = segment start + VEC * lane; lanes past the row's padding idle).  Called by the whole warp.
 template <int PREC>
-__global__ void __launch_bounds__(32 * VEC_ROWS, 4) k_nptl_vec(StepParams p)
+__device__ __forceinline__ void vec_row_segment(const StepParams &p, int y, int xv, int lane)
 {
     static_assert(PREC == F16S || PREC == BF16S, "2-byte shifted storage only");
-    const int lane = threadIdx.x;                              // blockDim.x == 32: a warp is a row segment
-    const int y = blockIdx.y * VEC_ROWS + threadIdx.y;
-    if (y >= p.H) return;                                      // uniform over the warp
-    const int xv = (blockIdx.x * 32 + lane) * VEC;
     const bool vec_ok = xv < p.P;
     const int x0 = vec_ok ? xv : p.P - VEC;                    // clamped: every lane loads inside the row
     const unsigned short *S = static_cast<const unsigned short *>(p.lat0);
@@ -274,6 +294,15 @@ __global__ void __launch_bounds__(32 * VEC_ROWS, 4) k_nptl_vec(StepParams p)
 #pragma unroll
     for (int d = 0; d < 9; ++d)
         *reinterpret_cast<uint4 *>(D + (size_t)d * p.N + row0 + x0) = make_uint4(r[d][0], r[d][1], r[d][2], r[d][3]);
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(32 * VEC_ROWS, 4) k_nptl_vec(StepParams p)
+{
+    const int lane = threadIdx.x;                              // blockDim.x == 32: a warp is a row segment
+    const int y = blockIdx.y * VEC_ROWS + threadIdx.y;
+    if (y >= p.H) return;                                      // uniform over the warp
+    vec_row_segment<PREC>(p, y, (blockIdx.x * 32 + lane) * VEC, lane);
 }
 
 // lptl: 1-D launch over n = x' + y' * P (padding columns x' >= W idle); each thread updates NY

@@ -245,24 +245,30 @@ def test_set_equilibrium_of_rest_state_is_the_rest_start(plbm, precision):
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
 
 
-def _batch_domains(plbm, n=5, seed=11):
+def _batch_domains(plbm, n=5, seed=11, wmax=140):
     rng = np.random.default_rng(seed)
     doms = []
     for i in range(n):
-        w, h = int(rng.integers(40, 140)), int(rng.integers(24, 90))
+        w, h = int(rng.integers(40, wmax)), int(rng.integers(24, 90))
         doms.append({"mask": plbm.porous_disks(w, h, seed + i, float(rng.uniform(0.6, 0.8))),
                      "relaxation_time": float(rng.uniform(0.55, 1.0)),
                      "inlet_density": float(rng.uniform(1.001, 1.05)), "outlet_density": 1.0})
     return doms
 
 
-@pytest.mark.parametrize("precision", ["f32", "f16s", "f64_q60"])
+@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s", "f64_q60"])
 @pytest.mark.parametrize("mode", ["persistent", "persistent_graph", "per_domain"])
-def test_batch_equals_independent_handlers(plbm, precision, mode):
-    """Every domain of a batch ends bit-identical to the same channel run alone by a handler."""
-    doms = _batch_domains(plbm)
+@pytest.mark.parametrize("wide", [False, True])
+@pytest.mark.parametrize("vec_rows", [False, True])
+def test_batch_equals_independent_handlers(plbm, precision, mode, wide, vec_rows):
+    """Every domain of a batch ends bit-identical to the same channel run alone by a handler.
+    `wide` draws widths up to 700, so a domain spans several tiles across (and several 256-node
+    row segments with the vectorised rows of the 2-byte batches)."""
+    if vec_rows and (precision in ("f32", "f64_q60") or mode == "per_domain"):
+        pytest.skip("vectorised rows are a tile option of the persistent 2-byte batches")
+    doms = _batch_domains(plbm, wmax=700 if wide else 140)
     b = plbm.Batch(doms, precision=precision)
-    b.set_tile(32, 4, 8)
+    b.set_tile(32, 4 + 256 * (2 if wide else 1) + (plbm.BATCH_TILE_VEC if vec_rows else 0), 8)
     steps = 150
     b.run(steps, mode=mode)
     for i, d in enumerate(doms):
@@ -278,15 +284,17 @@ def test_batch_equals_independent_handlers(plbm, precision, mode):
     b.close()
 
 
-def test_batch_autotune_keeps_results(plbm):
-    """Autotuning times real steps (7 tile shapes x 3 occupancies x 2 steps = 42) and results do not
-    depend on the tile shape (threads, rows per thread) it picks."""
-    doms = _batch_domains(plbm, n=3, seed=5)
-    a = plbm.Batch(doms, precision="f32")
+@pytest.mark.parametrize("precision", ["f32", "f16s"])
+def test_batch_autotune_keeps_results(plbm, precision):
+    """Autotuning times real steps (7 tile shapes x 3 occupancies x 2 steps, twice that for 2-byte
+    storage, which also tries vectorised rows) and results do not depend on the tile it picks."""
+    doms = _batch_domains(plbm, n=3, seed=5, wmax=600)
+    a = plbm.Batch(doms, precision=precision)
     a.autotune(steps=2)
     a.run(58)
-    ref = plbm.Batch(doms, precision="f32")
-    ref.run(100, mode="per_domain")
+    tuned = 2 * 21 * (2 if precision == "f16s" else 1)
+    ref = plbm.Batch(doms, precision=precision)
+    ref.run(tuned + 58, mode="per_domain")
     for i in range(len(doms)):
         for k in range(3):
             assert np.array_equal(a.result(i, k), ref.result(i, k))

@@ -28,6 +28,17 @@ def test_library_exports_every_declared_symbol(plbm):
     assert not missing, missing
 
 
+def test_python_constants_match_the_header(plbm):
+    text = open(os.path.join(ROOT, "include", "plbm_c.h")).read()
+    consts = {k: int(v, 0) for k, v in re.findall(r"\b(PLBM_[A-Z0-9_]+)\s*=\s*(0x[0-9a-fA-F]+|\d+)", text)}
+    consts.update({k: int(v, 0) for k, v in re.findall(r"#define\s+(PLBM_[A-Z0-9_]+)\s+(0x[0-9a-fA-F]+|\d+)", text)})
+    for name, code in plbm.PRECISIONS.items():
+        assert consts["PLBM_" + name.upper()] == code, name
+    for name, code in plbm.BATCH_MODES.items():
+        assert consts["PLBM_BATCH_" + name.upper()] == code, name
+    assert consts["PLBM_BATCH_TILE_VEC"] == plbm.BATCH_TILE_VEC
+
+
 def test_properties_ghost_accounting(plbm):
     """Properties ctor adds two ghost layers (simulation.cpp:45-48; test_properties.cpp:44-71)."""
     p = P(plbm, v=30, h=126)
