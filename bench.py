@@ -65,9 +65,10 @@ def peaks() -> dict:
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons every 200 ms while running."""
+    """Samples nvidia-smi clocks and throttle reasons every 100 ms while running; summary() keeps the
+    samples whose nvidia-smi timestamp falls inside the timed steps' wall-clock window."""
 
-    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
@@ -81,7 +82,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
         except Exception:
@@ -102,23 +103,39 @@ class ClockSampler:
         if self._t:
             self._t.join(timeout=2)
 
-    def summary(self) -> dict:
-        sm, smax, reasons = [], 0.0, set()
-        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+    def _samples(self):
+        import datetime
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 8:
+            if len(parts) < 9:
                 continue
             try:
-                sm.append(float(parts[0]))
-                smax = max(smax, float(parts[1]))
+                t = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                yield t, float(parts[1]), float(parts[2]), parts[5:9]
             except ValueError:
                 continue
-            for name, v in zip(names, parts[4:8]):
+
+    def summary(self, window=None) -> dict:
+        """window: (t0, t1) in time.time() seconds; samples outside it (set-up, warm-up) are dropped.
+        With no sample inside a short window, the samples within 0.3 s of it are used."""
+        samples = list(self._samples())
+        if window:
+            t0, t1 = window
+            inside = [x for x in samples if t0 <= x[0] <= t1]
+            samples = inside or [x for x in samples if t0 - 0.3 <= x[0] <= t1 + 0.3]
+        sm, smax, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for _, clk, cmax, flags in samples:
+            sm.append(clk)
+            smax = max(smax, cmax)
+            for name, v in zip(names, flags):
                 if v.lower() == "active":
                     reasons.add(name)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax or None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        out = {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax or None,
+               "reasons": sorted(reasons), "samples": len(sm)}
+        if window:
+            out["window_s"] = round(window[1] - window[0], 3)
+        return out
 
 
 def make_props(plbm, alg, lay, w, h, steps, fui=None, wg=1024):
@@ -126,14 +143,18 @@ def make_props(plbm, alg, lay, w, h, steps, fui=None, wg=1024):
                            0.0, 1.0, 0.6)
 
 
-def device_run(plbm, precision, alg, lay, w, h, mask, steps, warmup, tau=None):
-    """K device-resident steps; returns (ms_per_step, handler)."""
+def device_run(plbm, precision, alg, lay, w, h, mask, steps, warmup, tau=None, window=None):
+    """K device-resident steps; returns (ms_per_step, handler).  `window` (a list) receives the
+    wall-clock bounds of the timed steps (run_steps synchronises before it returns)."""
     props = make_props(plbm, alg, lay, w, h, steps + warmup + 10)
     if tau is not None:
         props.relaxation_time = float(tau)
     hd = plbm.create_handler(props, precision=precision, mask=mask)
     hd.run_steps(warmup)
+    t0 = time.time()
     ms = hd.run_steps(steps)
+    if window is not None:
+        window[:] = [t0, time.time()]
     return ms, hd
 
 
@@ -429,7 +450,7 @@ def run_reference(args, world, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--width", type=int, default=W_DEFAULT)
@@ -486,8 +507,10 @@ def main():
 
     # -- device-resident timed region (value + roofline) --
     barrier(world)
+    window = []
     with ClockSampler(local) as clocks:
-        ms, hd = device_run(plbm, args.precision, args.algorithm, args.layout, w, h, mask, args.steps, args.warmup)
+        ms, hd = device_run(plbm, args.precision, args.algorithm, args.layout, w, h, mask, args.steps, args.warmup,
+                            window=window)
     barrier(world)
     ms = max_over_ranks(ms, world)
     launches = hd.launches_per_step() * args.steps
@@ -554,7 +577,7 @@ def main():
             "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS", "h2d_bytes_per_step": round(w * h / e2e_steps),
                     "d2h_bytes_per_step": round(4 * 8 * w * h / e2e_steps)},
             "gpu_launches": launches,
-            "clocks": clocks.summary(),
+            "clocks": clocks.summary(window),
             "cpu_baseline": cpu,
             "variants": variants,
             "precision_study": study,

@@ -1,0 +1,29 @@
+"""Host-side pieces of bench.py that need no GPU: the clock record keeps only the samples taken
+while the timed steps ran."""
+import datetime
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+import bench  # noqa: E402
+
+
+def _line(t, sm, reasons=("Not Active",) * 4):
+    ts = datetime.datetime.fromtimestamp(t).strftime("%Y/%m/%d %H:%M:%S.%f")[:-3]
+    return ", ".join([ts, str(sm), "2070", "900.5", "0x0000000000000000", *reasons])
+
+
+def test_clock_summary_keeps_the_timed_window():
+    c = bench.ClockSampler(0)
+    t0 = 1_790_000_000.0
+    # set-up at low clock, timed steps at full clock, a throttle flag only during set-up
+    c.lines = ([_line(t0 + 0.1 * k, 1000, ("Active", "Not Active", "Not Active", "Not Active")) for k in range(10)]
+               + [_line(t0 + 1.0 + 0.1 * k, 1995 + k) for k in range(8)] + ["garbage line"])
+    whole = c.summary()
+    assert whole["samples"] == 18 and whole["reasons"] == ["hw_slowdown"]
+    timed = c.summary((t0 + 0.95, t0 + 1.75))
+    assert timed["samples"] == 8 and timed["reasons"] == [] and timed["sm_mhz"] == 1998.5
+    assert timed["sm_max_mhz"] == 2070 and timed["window_s"] == 0.8
+    # a window shorter than the sampling interval takes its neighbours within 0.3 s
+    short = c.summary((t0 + 1.72, t0 + 1.74))
+    assert short["samples"] == 3 and short["reasons"] == []
