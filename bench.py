@@ -204,12 +204,9 @@ def err_vs_oracle(plbm, precision, steps=2000, w=400, h=100):
     return float(max(np.max(np.abs(a - b)) for a, b in zip(got, ref)))
 
 
-# DRAM bytes (read + write) per step launch from one ncu capture of the 4096 x 4096 circle channel
-# (profiles/k_nptl_f64q60_stream_4096x4096.md, profiles/k_nptl_f64fast_stream_4096x4096.md), per
-# node; traffic is proportional to the node count at fixed geometry, so the bench scales it.
 # DRAM read + write bytes of one step launch, from ncu captures of the 4096^2 circle channel
 # (profiles/), per inner node; geometry scales with the domain, so traffic is proportional.
-TRAFFIC_PER_NODE = {"nptl_stream_f64_q60": 2.300e9 / (4096 * 4096), "nptl_stream_f64_fast": 2.283e9 / (4096 * 4096),
+TRAFFIC_PER_NODE = {"nptl_stream_f64_q60": 2.293e9 / (4096 * 4096), "nptl_stream_f64_fast": 2.283e9 / (4096 * 4096),
                     "nptl_stream_f32": 1.1375e9 / (4096 * 4096), "nptl_stream_f16s": 0.5923e9 / (4096 * 4096)}
 
 
