@@ -211,21 +211,22 @@ TRAFFIC_PER_NODE = {"nptl_stream_f64_q60": 2.293e9 / (4096 * 4096), "nptl_stream
 
 
 def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, max_steps=100000,
-                    big=(8192, 8192), big_steps=2000):
+                    big=(8192, 8192), big_steps=2000, big_cap=None, small=True):
     """Each storage form against the FP64 drop-in on a seeded porous channel (disks r in [3, 12],
     tau 0.6, rho 1.01 / 1.0): steps to residual `target`, relative L2 error of the momentum field
     and relative total-mass difference at steady state; then the same errors on the 8192^2 porous
-    channel after `big_steps` steps against f64_q60 (FP64 accuracy, <= 1e-12 from the drop-in)."""
+    channel against f64_q60 (FP64 accuracy, <= 1e-12 from the drop-in), after `big_steps` steps or,
+    with `big_cap`, run to `target` with at most `big_cap` steps (steps and residual recorded)."""
     mask = plbm.porous_disks(w, h, seed, porosity)
     fluid = mask.reshape(-1) == 0
 
-    def run(prec, mk, ww, hh, to_residual=True, steps=0):
+    def run(prec, mk, ww, hh, to_residual=True, steps=0, cap=max_steps):
         props = plbm.Properties("nptl", "stream", False, 1024, 10 ** 9, 10 ** 9, "Hagen-Poiseuille", hh, ww, 0.0,
                                 0.0, 1.01, 0.0, 0.0, 1.0, 0.6)
         hd = plbm.create_handler(props, precision=prec, mask=mk)
         t0 = time.perf_counter()
         if to_residual:
-            n, r = hd.run_to_residual(target, 100, max_steps)
+            n, r = hd.run_to_residual(target, 100, cap)
         else:
             hd.run_steps(steps)
             hd.sync_results()
@@ -241,23 +242,30 @@ def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, 
         return (float(np.linalg.norm(ja - jb) / np.linalg.norm(jb)),
                 float((a[0][fl].sum() - b[0][fl].sum()) / b[0][fl].sum()))
 
-    n64, r64, t64, ref = run("f64_strict", mask, w, h)
-    study = {"domain": f"{w}x{h} porous (seed {seed}, porosity {porosity})", "target_residual": target,
-             "f64_strict": {"steps": n64, "residual": r64, "seconds": round(t64, 3)}}
-    for prec in ("f64_q60", "f64_fast", "f32", "f16s", "bf16s"):
-        n, r, dt, out = run(prec, mask, w, h)
-        l2, dm = errs(out, ref, fluid)
-        study[prec] = {"steps": n, "residual": r, "seconds": round(dt, 3), "rel_l2_j_vs_f64": l2,
-                       "mass_rel_diff_vs_f64": dm}
+    study = {"target_residual": target}
+    if small:
+        n64, r64, t64, ref = run("f64_strict", mask, w, h)
+        study.update({"domain": f"{w}x{h} porous (seed {seed}, porosity {porosity})",
+                      "f64_strict": {"steps": n64, "residual": r64, "seconds": round(t64, 3)}})
+        for prec in ("f64_q60", "f64_fast", "f32", "f16s", "bf16s"):
+            n, r, dt, out = run(prec, mask, w, h)
+            l2, dm = errs(out, ref, fluid)
+            study[prec] = {"steps": n, "residual": r, "seconds": round(dt, 3), "rel_l2_j_vs_f64": l2,
+                           "mass_rel_diff_vs_f64": dm}
     bw, bh = big
     bmask = plbm.porous_disks(bw, bh, seed, porosity)
     bfl = bmask.reshape(-1) == 0
-    _, _, _, bref = run("f64_q60", bmask, bw, bh, False, big_steps)
-    study["large"] = {"domain": f"{bw}x{bh} porous, {big_steps} steps, against f64_q60"}
+    conv = big_cap is not None
+    nref, rref, tref, bref = run("f64_q60", bmask, bw, bh, conv, big_steps, big_cap or 0)
+    study["large"] = {"domain": f"{bw}x{bh} porous (seed {seed}, porosity {porosity}), against f64_q60",
+                      "f64_q60": {"steps": nref, "residual": rref, "seconds": round(tref, 1)}}
+    if not conv:
+        study["large"]["domain"] += f", {big_steps} steps"
     for prec in ("f32", "f16s", "bf16s"):
-        _, _, _, out = run(prec, bmask, bw, bh, False, big_steps)
+        n, r, dt, out = run(prec, bmask, bw, bh, conv, big_steps, big_cap or 0)
         l2, dm = errs(out, bref, bfl)
-        study["large"][prec] = {"rel_l2_j": l2, "mass_rel_diff": dm}
+        study["large"][prec] = {"steps": n, "residual": r, "seconds": round(dt, 1), "rel_l2_j": l2,
+                                "mass_rel_diff": dm}
     return study
 
 
@@ -466,6 +474,9 @@ def main():
     ap.add_argument("--warmstart-test", type=int, default=200)
     ap.add_argument("--warmstart-save", default=None, help="write the trained weights (.npz) here")
     ap.add_argument("--batch-study-only", action="store_true", help="only the batching study")
+    ap.add_argument("--precision-study-large", type=int, default=0, metavar="CAP",
+                    help="only the 8192^2 porous precision study, each form run to residual 1e-6 "
+                         "with at most CAP steps")
     ap.add_argument("--batch-domains", type=int, default=256)
     ap.add_argument("--nn-bench", action="store_true", help="only the warm-start operator's kernel timings")
     ap.add_argument("--sweep", action="store_true",
@@ -480,10 +491,13 @@ def main():
     import portlbm_gb300 as plbm
     from portlbm_gb300 import build as b
     b.build()
-    if args.batch_study_only or args.nn_bench or args.sweep:
+    if args.batch_study_only or args.nn_bench or args.sweep or args.precision_study_large:
         if rank == 0:
             if args.sweep:
                 key, res = "sweep", sweep(plbm)
+            elif args.precision_study_large:
+                key, res = "precision_study_large", precision_study(plbm, big_cap=args.precision_study_large,
+                                                                    small=False)
             else:
                 key, res = (("batch_study", batch_study(plbm, n=args.batch_domains)) if args.batch_study_only
                             else ("nn_bench", nn_bench()))

@@ -84,9 +84,21 @@ typedef struct {
     int device;             /* CUDA device ordinal */
     const int8_t *mask;     /* optional geometry: inner W*H flags (0 fluid, 1 solid), row-major
                                from (x=1, y=1); replaces walls + scenario stencil. Copied. */
+    int gather;             /* PLBM_GATHER_*: how nptl/lptl gather the nodes next to obstacles in
+                               the f32/f16s/bf16s forms (same results either way) */
 } plbm_options;
 
+/* PLBM_GATHER_OPEN: branch to the per-direction gather (and, for f16s/bf16s nptl/stream, the
+ * vectorised rows), fastest when obstacles are rare; PLBM_GATHER_POROUS: one selected load per
+ * direction for every interior node, fastest when most warps hold an obstacle; PLBM_GATHER_AUTO:
+ * porous when more than PLBM_GATHER_POROUS_FRACTION of the 32-node row segments holding fluid
+ * mix interior nodes next to a solid with nodes that are not. */
+enum { PLBM_GATHER_AUTO = 0, PLBM_GATHER_OPEN = 1, PLBM_GATHER_POROUS = 2 };
+#define PLBM_GATHER_POROUS_FRACTION 0.04
+
 void plbm_default_options(plbm_options *opt);
+/* The gather the handler runs (PLBM_GATHER_OPEN or PLBM_GATHER_POROUS, AUTO resolved). */
+int plbm_gather_form(plbm_handler *h, int *form);
 
 /* Validates like core::Properties::validate() (src/lbm/core/simulation.cpp:60-125) without
  * touching a GPU. */

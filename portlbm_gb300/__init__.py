@@ -76,7 +76,11 @@ class _CProps(ctypes.Structure):
 
 class _COpts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("nan_protection", ctypes.c_int), ("use_graph", ctypes.c_int),
-                ("device", ctypes.c_int), ("mask", ctypes.c_void_p)]
+                ("device", ctypes.c_int), ("mask", ctypes.c_void_p), ("gather", ctypes.c_int)]
+
+
+# PLBM_GATHER_*: the gather of obstacle-adjacent nodes in the f32/f16s/bf16s nptl/lptl steps
+GATHER = {"auto": 0, "open": 1, "porous": 2}
 
 
 def library_path() -> str:
@@ -109,6 +113,7 @@ _SIGS = {
     "plbm_json_to_properties": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_CProps)]),
     "plbm_run_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint, ctypes.POINTER(ctypes.c_double)]),
     "plbm_sync_results": (ctypes.c_int, [ctypes.c_void_p]),
+    "plbm_gather_form": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "plbm_launches_per_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint)]),
     "plbm_bytes_per_node": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "plbm_mass_momentum": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
@@ -417,6 +422,12 @@ class AlgorithmHandler:
         self._call("plbm_bytes_per_node", ctypes.byref(v))
         return v.value
 
+    def gather_form(self) -> str:
+        """The gather the step runs: "open" or "porous"."""
+        v = ctypes.c_int()
+        self._call("plbm_gather_form", ctypes.byref(v))
+        return {1: "open", 2: "porous"}[v.value]
+
     def launches_per_step(self) -> int:
         v = ctypes.c_uint()
         self._call("plbm_launches_per_step", ctypes.byref(v))
@@ -543,15 +554,18 @@ def run_benchmark(settings_path, benchmark_path=None, output_root=None, precisio
 
 
 def create_handler(source, precision: str = "f64_strict", mask=None, nan_protection: bool = True,
-                   use_graph: bool = True, device: int = 0) -> AlgorithmHandler:
+                   use_graph: bool = True, device: int = 0, gather: str = "auto") -> AlgorithmHandler:
     """lbm::create_handler from a ``Properties`` or a settings.json path.
 
     ``precision`` picks the arithmetic form ("f64_strict" is the drop-in); ``mask`` is an optional
-    (H, W) array of 0 (fluid) / 1 (solid) replacing walls and scenario geometry.
+    (H, W) array of 0 (fluid) / 1 (solid) replacing walls and scenario geometry; ``gather``
+    ("auto", "open", "porous") picks how the f32/f16s/bf16s steps gather obstacle-adjacent nodes
+    (same results; "auto" decides from the geometry).
     """
     lib = load_library()
     opts = _COpts()
     lib.plbm_default_options(ctypes.byref(opts))
+    opts.gather = GATHER[gather]
     opts.precision = PRECISIONS[precision]
     opts.nan_protection = int(bool(nan_protection))
     opts.use_graph = int(bool(use_graph))

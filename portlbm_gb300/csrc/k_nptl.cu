@@ -3,8 +3,15 @@
 #include "plbm_launch.h"
 
 namespace plbm {
-cudaError_t launch_nptl(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s)
+cudaError_t launch_nptl(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s, bool porous)
 {
+    if (porous && prec >= F32 && prec <= BF16S) {
+        switch (prec * 3 + lay) {
+            PLBM_POROUS_CASES(k_nptl)
+        default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
     // 2-byte storage in the stream layout: vectorised rows (launch shape of its own)
     if ((prec == F16S || prec == BF16S) && lay == STREAM) {
         const dim3 vb(32, VEC_ROWS), vg((unsigned)((p.P + 32 * VEC - 1) / (32 * VEC)), (unsigned)((p.H + VEC_ROWS - 1) / VEC_ROWS));

@@ -413,6 +413,7 @@ struct plbm_handler {
     int W = 0, H = 0, P = 0;
     unsigned long long N = 0;
     int outlet_mode = 0;
+    bool porous = false;   // nptl/lptl shifted forms: the obstacle-select gather (PLBM_GATHER_POROUS)
 
     cudaStream_t stream = nullptr;
     void *lat[2] = { nullptr, nullptr };
@@ -604,6 +605,13 @@ struct plbm_handler {
         cuda_check(cudaMemcpyAsync(flags_d, flags_src, nres, cudaMemcpyHostToDevice, stream), "H2D flags");
         if (has_mask) cuda_check(plbm::launch_check_mask(flags_d, nres, status_d, stream), "mask check");
         cuda_check(plbm::launch_links(flags_d, links, W, H, P, stream), "links kernel");
+        if (opt.gather < PLBM_GATHER_AUTO || opt.gather > PLBM_GATHER_POROUS)
+            fail(PLBM_ERR_ARGUMENT, "gather must be PLBM_GATHER_AUTO, PLBM_GATHER_OPEN or PLBM_GATHER_POROUS");
+        const bool count_obstacles = opt.gather == PLBM_GATHER_AUTO && alg <= 1 &&
+                                     (prec == PLBM_F32 || prec == PLBM_F16S || prec == PLBM_BF16S);
+        if (count_obstacles)   // read after the initialisation sync below
+            cuda_check(plbm::launch_count_obstacle_nodes(links, W, H, P, reinterpret_cast<unsigned long long *>(red_d),
+                                                         stream), "obstacle count");
         cuda_check(plbm::launch_fill_results(res_d[0], res_d[1], res_d[2], res_d[3], nres, stream), "results fill");
 
         // Ghost constants and rest state in the arithmetic of the chosen form.
@@ -693,6 +701,12 @@ struct plbm_handler {
             }
         }
         cuda_check(cudaStreamSynchronize(stream), "initialisation");
+        porous = opt.gather == PLBM_GATHER_POROUS;
+        if (count_obstacles) {
+            unsigned long long c[2] = { 0, 0 };
+            cuda_check(cudaMemcpy(c, red_d, sizeof c, cudaMemcpyDeviceToHost), "obstacle count");
+            porous = (double)c[1] > PLBM_GATHER_POROUS_FRACTION * (double)c[0];
+        }
         if (has_mask) {
             int bad = 0;
             cuda_check(cudaMemcpy(&bad, status_d, sizeof(int), cudaMemcpyDeviceToHost), "mask check");
@@ -714,8 +728,8 @@ struct plbm_handler {
         p.jy_next = jy_d + (size_t)(par ^ 1u) * H;
         if (alg == 2) { p.halo_in = (double *)halo[par]; p.halo_out = (double *)halo[par ^ 1u]; }
         switch (alg) {
-        case 0: return plbm::launch_nptl(prec, lay, p, grid, block, stream);
-        case 1: return plbm::launch_lptl(prec, lay, p, grid, block, stream);
+        case 0: return plbm::launch_nptl(prec, lay, p, grid, block, stream, porous);
+        case 1: return plbm::launch_lptl(prec, lay, p, grid, block, stream, porous);
         case 2: return plbm::launch_npol(prec, lay, p, grid, block, stream);
         default: return plbm::launch_nsol(prec, lay, p, t, grid, block, stream);
         }
@@ -920,6 +934,15 @@ void plbm_default_options(plbm_options *o)
     o->use_graph = 1;
     o->device = 0;
     o->mask = nullptr;
+    o->gather = PLBM_GATHER_AUTO;
+}
+
+int plbm_gather_form(plbm_handler *h, int *form)
+{
+    return guarded(h, [&] {
+        if (!form) fail(PLBM_ERR_ARGUMENT, "form is NULL");
+        *form = h->porous ? PLBM_GATHER_POROUS : PLBM_GATHER_OPEN;
+    });
 }
 
 int plbm_validate(const plbm_properties *props)

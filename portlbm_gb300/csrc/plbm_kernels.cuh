@@ -152,7 +152,7 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
 template <int PREC> struct NptlBounds { static constexpr int threads = 512, blocks = 1; };
 template <> struct NptlBounds<F64_Q60> { static constexpr int threads = 256, blocks = 5; };
 
-template <int PREC, int L>
+template <int PREC, int L, bool POROUS = false>
 __global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::blocks) k_nptl(StepParams p)
 {
     constexpr int NY = RowsPerThread<PREC>::value;
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::b
     int xi[NY], yi[NY];
 #pragma unroll
     for (int j = 0; j < NY; ++j) { xi[j] = x; yi[j] = y0 + j; }
-    update_two_lattice_rows<PREC, L, NY>(xi, yi, p);
+    update_two_lattice_rows<PREC, L, NY, POROUS>(xi, yi, p);
 }
 
 // nptl, stream layout, 2-byte storage (F16S / BF16S): each thread updates VEC consecutive nodes
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(32 * VEC_ROWS, 4) k_nptl_vec(StepParams p)
 
 // lptl: 1-D launch over n = x' + y' * P (padding columns x' >= W idle); each thread updates NY
 // nodes one grid-width apart.
-template <int PREC, int L>
+template <int PREC, int L, bool POROUS = false>
 __global__ void k_lptl(StepParams p)
 {
     constexpr int NY = RowsPerThread<PREC>::value;
@@ -325,7 +325,7 @@ __global__ void k_lptl(StepParams p)
             xi[j] = p.W;
         }
     }
-    update_two_lattice_rows<PREC, L, NY>(xi, yi, p);
+    update_two_lattice_rows<PREC, L, NY, POROUS>(xi, yi, p);
 }
 
 // ---- npol: in place, one tile per thread block --------------------------------------------

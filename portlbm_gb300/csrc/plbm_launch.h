@@ -8,8 +8,13 @@ namespace plbm {
 
 // One timestep of algorithm `alg` (0 nptl, 1 lptl, 2 npol, 3 nsol) for precision `prec` and
 // layout `lay`; `t` is the absolute step index (selects the nsol parity kernel).
-cudaError_t launch_nptl(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s);
-cudaError_t launch_lptl(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s);
+// porous: the obstacle-select gather of the shifted forms (f32, f16s, bf16s)
+cudaError_t launch_nptl(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s, bool porous);
+cudaError_t launch_lptl(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s, bool porous);
+// counts[0] = 32-node row segments holding fluid, counts[1] = those mixing interior nodes with and
+// without a solid neighbour
+cudaError_t launch_count_obstacle_nodes(const uint16_t *links, int W, int H, int P, unsigned long long *counts,
+                                        cudaStream_t s);
 cudaError_t launch_npol(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s);
 cudaError_t launch_nsol(int prec, int lay, const StepParams &p, unsigned t, dim3 grid, dim3 block, cudaStream_t s);
 

@@ -48,6 +48,38 @@ cudaError_t launch_links(const int8_t *flags, uint16_t *links, int W, int H, int
     return cudaGetLastError();
 }
 
+// Over the 32-node row segments (P is a multiple of 32, so a warp's 32 consecutive nodes are one
+// segment): counts[0] += segments holding fluid, counts[1] += segments whose interior fluid nodes
+// mix both kinds, all sources fluid and some source solid (a warp that splits between gathers).
+__global__ void k_count_obstacle_nodes(const uint16_t *links, int W, int H, int P, unsigned long long *counts)
+{
+    unsigned seg = 0, mixed = 0;
+    const unsigned long long n = (unsigned long long)P * H;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;   // a multiple of 32
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint16_t lk = links[i];   // the loop bound is warp-uniform: n is a multiple of 32
+        const unsigned fl = __ballot_sync(0xffffffffu, (lk & LINK_FLUID) != 0);
+        const unsigned plain = __ballot_sync(0xffffffffu, lk == LINK_FLUID);
+        const unsigned near = __ballot_sync(0xffffffffu, (lk & (LINK_FLUID | LINK_EDGE)) == LINK_FLUID && lk != LINK_FLUID);
+        seg += fl != 0;
+        mixed += plain != 0 && near != 0;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&counts[0], (unsigned long long)seg);
+        atomicAdd(&counts[1], (unsigned long long)mixed);
+    }
+    (void)W;
+}
+
+cudaError_t launch_count_obstacle_nodes(const uint16_t *links, int W, int H, int P, unsigned long long *counts,
+                                        cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(counts, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    k_count_obstacle_nodes<<<152 * 4, 256, 0, s>>>(links, W, H, P, counts);
+    return cudaGetLastError();
+}
+
 struct W9 { double w[9]; };
 
 template <int PREC>

@@ -15,10 +15,10 @@ pytestmark = pytest.mark.gpu
 
 
 def run_gpu(plbm, alg, lay, scenario, w, h, steps, wg=64, precision="f64_strict", rho_in=1.05, tau=0.6, mask=None,
-            fui=None):
+            fui=None, gather="auto"):
     props = plbm.Properties(alg, lay, False, wg, steps, fui or steps, scenario, h, w, 0.0, 0.0, rho_in, 0.0, 0.0,
                             1.0, tau)
-    hd = plbm.create_handler(props, precision=precision, mask=mask)
+    hd = plbm.create_handler(props, precision=precision, mask=mask, gather=gather)
     hd.start()
     hd.block_until_finished()
     out = {"rho": hd.get_densities(), "jx": hd.get_x_velocities(), "jy": hd.get_y_velocities(),
@@ -64,16 +64,39 @@ def test_q60_within_tolerance(plbm, oracle_mod, alg, lay):
 @pytest.mark.parametrize("precision", ["f16s", "bf16s"])
 @pytest.mark.parametrize("w,h,porous", [(203, 61, True), (300, 40, True), (62, 30, False), (520, 20, True)])
 def test_vectorised_rows_match_scalar_kernel(plbm, precision, w, h, porous):
-    """nptl/stream runs the 2-byte forms 8 nodes per thread with warp shuffles; lptl and the
-    collision layout run the scalar gather: same arithmetic, bit-identical results (row lengths
-    not a multiple of 8 or 256, porous obstacles, inlet, outlet, walls)."""
+    """nptl/stream runs the 2-byte forms 8 nodes per thread with warp shuffles (open gather); lptl,
+    the collision layout and the porous gather run the scalar kernels: same arithmetic,
+    bit-identical results (row lengths not a multiple of 8 or 256, porous obstacles, inlet,
+    outlet, walls)."""
     mask = plbm.porous_disks(w, h, 9, 0.7) if porous else None
     scen = "Hagen-Poiseuille" if porous else "circle"
-    a = run_gpu(plbm, "nptl", "stream", scen, w, h, 300, precision=precision, mask=mask)
-    b = run_gpu(plbm, "lptl", "stream", scen, w, h, 300, precision=precision, mask=mask)
-    c = run_gpu(plbm, "nptl", "collision", scen, w, h, 300, precision=precision, mask=mask)
+    a = run_gpu(plbm, "nptl", "stream", scen, w, h, 300, precision=precision, mask=mask, gather="open")
+    others = [run_gpu(plbm, alg, lay, scen, w, h, 300, precision=precision, mask=mask, gather=g)
+              for alg, lay, g in (("lptl", "stream", "open"), ("nptl", "collision", "open"),
+                                  ("nptl", "stream", "porous"), ("lptl", "bundle", "porous"))]
     for k in a:
-        assert np.array_equal(a[k], b[k]) and np.array_equal(a[k], c[k]), k
+        for b in others:
+            assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("precision", ["f32", "f16s", "f64_strict"])
+@pytest.mark.parametrize("alg,lay", [("nptl", "stream"), ("nptl", "bundle"), ("lptl", "collision")])
+def test_gather_forms_agree(plbm, precision, alg, lay):
+    """The open and the porous gather give bit-identical results on a porous channel; "auto"
+    takes the porous gather there and the open one in a channel with a single disk (the FP64
+    forms have one gather)."""
+    w, h = 157, 53
+    mask = plbm.porous_disks(w, h, 4, 0.7)
+    a = run_gpu(plbm, alg, lay, "Hagen-Poiseuille", w, h, 250, precision=precision, mask=mask, gather="open")
+    b = run_gpu(plbm, alg, lay, "Hagen-Poiseuille", w, h, 250, precision=precision, mask=mask, gather="porous")
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    props = plbm.Properties(alg, lay, False, 64, 10, 10, "Hagen-Poiseuille", h, w, 0.0, 0.0, 1.05, 0.0, 0.0, 1.0, 0.6)
+    shifted = precision != "f64_strict"
+    for m, want in ((mask, "porous" if shifted else "open"), (None, "open")):
+        hd = plbm.create_handler(props, precision=precision, mask=m)
+        assert hd.gather_form() == want
+        hd.close()
 
 
 def test_q60_rejects_out_of_range_boundary(plbm):

@@ -37,6 +37,8 @@ def test_python_constants_match_the_header(plbm):
     for name, code in plbm.BATCH_MODES.items():
         assert consts["PLBM_BATCH_" + name.upper()] == code, name
     assert consts["PLBM_BATCH_TILE_VEC"] == plbm.BATCH_TILE_VEC
+    for name, code in plbm.GATHER.items():
+        assert consts["PLBM_GATHER_" + name.upper()] == code, name
 
 
 def test_properties_ghost_accounting(plbm):
