@@ -607,8 +607,9 @@ struct plbm_handler {
         cuda_check(plbm::launch_links(flags_d, links, W, H, P, stream), "links kernel");
         if (opt.gather < PLBM_GATHER_AUTO || opt.gather > PLBM_GATHER_POROUS)
             fail(PLBM_ERR_ARGUMENT, "gather must be PLBM_GATHER_AUTO, PLBM_GATHER_OPEN or PLBM_GATHER_POROUS");
-        const bool count_obstacles = opt.gather == PLBM_GATHER_AUTO && alg <= 1 &&
-                                     (prec == PLBM_F32 || prec == PLBM_F16S || prec == PLBM_BF16S);
+        // only the shifted forms of nptl/lptl have a porous instantiation
+        const bool has_porous = alg <= 1 && (prec == PLBM_F32 || prec == PLBM_F16S || prec == PLBM_BF16S);
+        const bool count_obstacles = has_porous && opt.gather == PLBM_GATHER_AUTO;
         if (count_obstacles)   // read after the initialisation sync below
             cuda_check(plbm::launch_count_obstacle_nodes(links, W, H, P, reinterpret_cast<unsigned long long *>(red_d),
                                                          stream), "obstacle count");
@@ -701,7 +702,7 @@ struct plbm_handler {
             }
         }
         cuda_check(cudaStreamSynchronize(stream), "initialisation");
-        porous = opt.gather == PLBM_GATHER_POROUS;
+        porous = has_porous && opt.gather == PLBM_GATHER_POROUS;
         if (count_obstacles) {
             unsigned long long c[2] = { 0, 0 };
             cuda_check(cudaMemcpy(c, red_d, sizeof c, cudaMemcpyDeviceToHost), "obstacle count");

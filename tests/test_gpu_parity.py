@@ -93,8 +93,9 @@ def test_gather_forms_agree(plbm, precision, alg, lay):
         assert np.array_equal(a[k], b[k]), k
     props = plbm.Properties(alg, lay, False, 64, 10, 10, "Hagen-Poiseuille", h, w, 0.0, 0.0, 1.05, 0.0, 0.0, 1.0, 0.6)
     shifted = precision != "f64_strict"
-    for m, want in ((mask, "porous" if shifted else "open"), (None, "open")):
-        hd = plbm.create_handler(props, precision=precision, mask=m)
+    for m, g, want in ((mask, "auto", "porous" if shifted else "open"), (None, "auto", "open"),
+                       (None, "porous", "porous" if shifted else "open")):
+        hd = plbm.create_handler(props, precision=precision, mask=m, gather=g)
         assert hd.gather_form() == want
         hd.close()
 
