@@ -560,9 +560,10 @@ struct plbm_handler {
         P = (W + 31) / 32 * 32;
         N = (unsigned long long)P * H;
         nres = (size_t)W * H;
-        // Buffered outlet border lookup (buffered.hpp:285-288) lands on a buffer column when the
-        // column X-3 closes a subdomain; the density outlet then never reaches the lattice and the
-        // outlet ghost keeps feq(outlet) (see the design doc for the derivation).
+        // Buffered outlet border lookup (buffered.hpp:285-288): the border is taken as
+        // BufferedNodeAccess(X-3, y) + 1, which is a buffer column when (X-3) is a multiple of the
+        // subdomain width; the outlet's writes then land on the border nodes' own populations
+        // (overwritten by their collision) and the outlet ghost keeps feq(outlet).
         outlet_mode = 0;
         if ((alg == 2 || alg == 3) && ((props.horizontal_nodes - 3) % dom.subdomain_horizontal_nodes) == 0) outlet_mode = 1;
 
