@@ -354,24 +354,29 @@ __global__ void k_npol(StepParams p)
     const unsigned long long n = inside ? (unsigned long long)xi + (unsigned long long)yi * p.P : 0;
     const uint16_t lk = inside ? p.links[n] : 0;
     const bool fluid = (lk & LINK_FLUID) != 0;
+    const int lx = threadIdx.x, ly = threadIdx.y;
     CT<PREC> f[9];
     if (fluid) {
+        if (lk == LINK_FLUID && lx > 0 && lx < TW - 1 && ly > 0 && ly < TH - 1) {
+            // inside the tile, away from the domain edge, all sources fluid
 #pragma unroll
-        for (int d = 0; d < 9; ++d) {
-            const int sx = xi - cxd(d), sy = yi - cyd(d);
-            if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H || (lk & (1u << d)) || d == 4) {
-                f[d] = pull_one<PREC, L>(p.lat0, n, xi, yi, d, lk, p);
-            } else if (sx / TW != tcx) {
-                const int k = sx < xi ? d / 3 : 3 + d / 3;
-                const int b = sx < xi ? sx / TW : tcx;
-                f[d] = ld<PREC>(p.halo_in, halo_col(p, b, sy, k), d, p);
-            } else if (sy / TH != tcy) {
-                const int k = sy < yi ? d - 6 : 3 + d;
-                const int b = sy < yi ? sy / TH : tcy;
-                f[d] = ld<PREC>(p.halo_in, halo_row(p, b, sx, k), d, p);
-            } else {
-                const unsigned long long s = (unsigned long long)sx + (unsigned long long)sy * p.P;
-                f[d] = ld<PREC>(p.lat0, lidx<L>(s, d, p.N), d, p);
+            for (int d = 0; d < 9; ++d) f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N) + pull_delta<L>(d, p), d, p);
+        } else {
+#pragma unroll
+            for (int d = 0; d < 9; ++d) {
+                const int cx = cxd(d), cy = cyd(d), sx = xi - cx, sy = yi - cy;
+                if (sx < 0 || sx >= p.W || sy < 0 || sy >= p.H || (lk & (1u << d)) || d == 4) {
+                    f[d] = pull_one<PREC, L>(p.lat0, n, xi, yi, d, lk, p);
+                } else if ((cx == 1 && lx == 0) || (cx == -1 && lx == TW - 1)) {
+                    // the source lies in the neighbouring tile column: its boundary snapshot
+                    const int k = cx == 1 ? d / 3 : 3 + d / 3;
+                    f[d] = ld<PREC>(p.halo_in, halo_col(p, cx == 1 ? tcx - 1 : tcx, sy, k), d, p);
+                } else if ((cy == 1 && ly == 0) || (cy == -1 && ly == TH - 1)) {
+                    const int k = cy == 1 ? d - 6 : 3 + d;
+                    f[d] = ld<PREC>(p.halo_in, halo_row(p, cy == 1 ? tcy - 1 : tcy, sx, k), d, p);
+                } else {
+                    f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N) + pull_delta<L>(d, p), d, p);
+                }
             }
         }
     }
@@ -381,7 +386,6 @@ __global__ void k_npol(StepParams p)
     const auto m = collide<PREC>(f, p);
 #pragma unroll
     for (int d = 0; d < 9; ++d) st<PREC>(p.lat0, lidx<L>(n, d, p.N), d, f[d], p);
-    const int lx = threadIdx.x, ly = threadIdx.y;
     if (lx == TW - 1 && tcx < p.n_col_bounds)
         for (int k = 0; k < 3; ++k) st<PREC>(p.halo_out, halo_col(p, tcx, yi, k), 3 * k + 2, f[3 * k + 2], p);
     if (lx == 0 && tcx > 0)
