@@ -153,8 +153,8 @@ cudaError_t launch_fill_shifted(void *lat, int prec, int lay, int P, unsigned lo
     return cudaGetLastError();
 }
 
-// Halo snapshot entries hold the rest state initially; the direction of each slot follows the
-// layout documented at k_npol.
+// Halo snapshot entries hold the rest state initially (w_d, or 0 for the shifted forms, whose
+// npol lattice stores f - w_d); the direction of each slot follows the layout documented at k_npol.
 template <int PREC>
 __global__ void k_fill_halo(void *halo, unsigned long long ncol, unsigned long long total, W9 w)
 {
@@ -169,6 +169,7 @@ __global__ void k_fill_halo(void *halo, unsigned long long ncol, unsigned long l
         if constexpr (PREC == F64_Q60) b[i] = double_to_q(w.w[d]);
         else if constexpr (PREC == F16S) b[i] = __float2half_rn(0.0f);
         else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(0.0f);
+        else if constexpr (PREC == F32) b[i] = 0.0f;
         else b[i] = (T)w.w[d];
     }
 }
@@ -182,7 +183,8 @@ cudaError_t launch_fill_halo(void *halo, int prec, int W, int H, int ncb, int nr
     const int grid = 152 * 2, block = 256;
     switch (prec) {
     case F64_STRICT: case F64_FAST: k_fill_halo<F64_STRICT><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
-    case F32_REF: case F32: k_fill_halo<F32><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
+    case F32_REF: k_fill_halo<F32_REF><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
+    case F32: k_fill_halo<F32><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
     case F16S: k_fill_halo<F16S><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
     case BF16S: k_fill_halo<BF16S><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
     case F64_Q60: k_fill_halo<F64_Q60><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
