@@ -106,16 +106,17 @@ SHIFTED_TOL = {"f32": (1e-4, 2e-6), "f16s": (2e-3, 2e-4), "bf16s": (2e-2, 2e-3)}
 
 @pytest.mark.parametrize("alg", ALGS)
 @pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s"])
-@pytest.mark.parametrize("porous", [False, True])
-def test_shifted_forms_track_fp64(plbm, alg, precision, porous):
-    """Every algorithm in the FP32/FP16/BF16 storage forms stays within its storage precision of
-    the FP64 drop-in (circle channel and a porous mask; nptl/lptl re-reference to the inlet-outlet
-    profile, npol/nsol to rho0 = 1 and keep halo snapshots and swapped slots in that form)."""
+@pytest.mark.parametrize("lay,porous", [("stream", False), ("stream", True), ("collision", True), ("bundle", False)])
+def test_shifted_forms_track_fp64(plbm, alg, precision, lay, porous):
+    """Every algorithm and data layout in the FP32/FP16/BF16 storage forms stays within its storage
+    precision of the FP64 drop-in (circle channel and a porous mask; nptl/lptl re-reference to the
+    inlet-outlet profile, npol/nsol to rho0 = 1 and keep halo snapshots and swapped slots in that
+    form)."""
     w, h = 203, 61
     mask = plbm.porous_disks(w, h, 9, 0.8) if porous else None
     scen = "Hagen-Poiseuille" if porous else "circle"
-    ref = run_gpu(plbm, alg, "stream", scen, w, h, 600, mask=mask)
-    got = run_gpu(plbm, alg, "stream", scen, w, h, 600, precision=precision, mask=mask)
+    ref = run_gpu(plbm, alg, lay, scen, w, h, 600, mask=mask)
+    got = run_gpu(plbm, alg, lay, scen, w, h, 600, precision=precision, mask=mask)
     jr = np.concatenate([ref["jx"], ref["jy"]])
     jg = np.concatenate([got["jx"], got["jy"]])
     l2, drho = np.linalg.norm(jg - jr) / np.linalg.norm(jr), np.abs(got["rho"] - ref["rho"]).max()
