@@ -71,12 +71,6 @@ __device__ __forceinline__ void emit_observables(const MomentsOf<PREC> &m, int x
     }
 }
 
-// Nodes away from the domain edge whose eight sources are all fluid take no per-direction checks.
-__device__ __forceinline__ bool interior_fluid(int xi, int yi, uint16_t lk, const StepParams &p)
-{
-    return lk == LINK_FLUID && xi > 0 && xi < p.W - 1 && yi > 0 && yi < p.H - 1;
-}
-
 // Rows per thread: a node of the 2-byte forms moves only 36 B, so each thread issues the loads of
 // several nodes before computing any of them to keep enough bytes in flight per SM.
 template <int PREC> struct RowsPerThread { static constexpr int value = rows_per_thread(PREC); };
@@ -216,7 +210,7 @@ __device__ __forceinline__ void vec_node(float f[9], int x, int y, uint16_t lk, 
                                          const StepParams &p)
 {
     if (live) {
-        // links carry LINK_EDGE on the domain's edge, so this is interior_fluid() in one compare
+        // lk == LINK_FLUID: fluid, every source fluid, off the domain edge (links carry LINK_EDGE)
         if (lk != LINK_FLUID) vec_edge_gather<PREC>(f, x, y, lk, p);
         const MomentsF m = collide<PREC>(f, p);
         emit_observables<PREC>(m, x, y, p);
@@ -413,7 +407,7 @@ __global__ void k_nsol_even(StepParams p)
     const uint16_t lk = p.links[n];
     if (!(lk & LINK_FLUID)) return;
     CT<PREC> f[9];
-    const bool fast = interior_fluid(xi, yi, lk, p);
+    const bool fast = lk == LINK_FLUID;   // links carry LINK_EDGE on the domain edge
     if (fast) {
 #pragma unroll
         for (int d = 0; d < 9; ++d) f[d] = ld<PREC>(p.lat0, lidx<L>(n, 8 - d, p.N) + pull_delta<L>(d, p), 8 - d, p);
@@ -460,7 +454,7 @@ __global__ void k_nsol_odd(StepParams p)
     const uint16_t lk = p.links[n];
     if (!(lk & LINK_FLUID)) return;
     CT<PREC> f[9];
-    if (interior_fluid(xi, yi, lk, p)) {
+    if (lk == LINK_FLUID) {   // links carry LINK_EDGE on the domain edge
 #pragma unroll
         for (int d = 0; d < 9; ++d) f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N), d, p);
     } else {
