@@ -141,8 +141,9 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
 
 // nptl: 2-D blocks (tile shape from the work-group size hint); each thread updates NY
 // consecutive rows of its column.
-// Launch bounds of the 2-D step kernel: the Q60 form runs 256-thread blocks and is limited by
-// memory latency, so it is held to 48 registers for a fifth resident block per SM.
+// Launch bounds of the nptl, lptl and npol step kernels: the Q60 form runs 256-thread blocks and
+// is limited by memory latency, so it is held to 48 registers for a fifth resident block per SM
+// (measured faster despite a few spilled words; nsol measured equal and keeps its registers).
 template <int PREC> struct NptlBounds { static constexpr int threads = 512, blocks = 1; };
 template <> struct NptlBounds<F64_Q60> { static constexpr int threads = 256, blocks = 5; };
 
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(32 * VEC_ROWS, 4) k_nptl_vec(StepParams p)
 // lptl: 1-D launch over n = x' + y' * P (padding columns x' >= W idle); each thread updates NY
 // nodes one grid-width apart.
 template <int PREC, int L, bool POROUS = false>
-__global__ void k_lptl(StepParams p)
+__global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::blocks) k_lptl(StepParams p)
 {
     constexpr int NY = RowsPerThread<PREC>::value;
     const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
@@ -339,7 +340,7 @@ __device__ __forceinline__ unsigned long long halo_row(const StepParams &p, int 
 }
 
 template <int PREC, int L>
-__global__ void k_npol(StepParams p)
+__global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::blocks) k_npol(StepParams p)
 {
     const int TW = p.tile_w, TH = p.tile_h;
     const int tcx = blockIdx.x, tcy = blockIdx.y;
