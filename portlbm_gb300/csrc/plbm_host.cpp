@@ -680,10 +680,12 @@ struct plbm_handler {
             block = dim3(t);
             grid = dim3((unsigned)((N + (unsigned long long)t * ny - 1) / ((unsigned long long)t * ny)));
         } else {
-            // nptl: rows of up to 128 nodes per block (wider rows per warp group measured faster
-            // than the subdomain's 32 for the float forms, equal for f64_q60); the hint sets the height
-            unsigned bx = alg == 0 ? std::min(128u, (unsigned)((W + 31) / 32 * 32))
-                                   : alg == 3 ? std::max(32u, std::min(sh, 128u)) : std::min(sh, 64u);
+            // nptl in the stream and bundle layouts: rows of up to 128 nodes per block (measured
+            // faster than the subdomain's 32 for the float forms, equal for f64_q60; the collision
+            // layout measured 5 % slower with them); the hint sets the height
+            unsigned bx = alg == 0 && lay != 0 ? std::min(128u, (unsigned)((W + 31) / 32 * 32))
+                                               : alg == 0 || alg == 3 ? std::max(32u, std::min(sh, 128u))
+                                                                      : std::min(sh, 64u);
             bx = std::max(1u, bx);
             unsigned by = std::max(1u, std::min(sv, (unsigned)cap / bx));
             if (alg == 2) {   // npol: one tile per block; tile edges carry the halo snapshots
