@@ -27,3 +27,19 @@ def test_clock_summary_keeps_the_timed_window():
     # a window shorter than the sampling interval takes its neighbours within 0.3 s
     short = c.summary((t0 + 1.72, t0 + 1.74))
     assert short["samples"] == 3 and short["reasons"] == []
+
+
+def test_reference_arm_samples_a_band_when_the_run_would_be_long(capsys):
+    """The reference arm (the CPU oracle) keeps each step a bounded sample: with a run that would
+    exceed its time budget it steps a centred band of the channel and says so in `sample`."""
+    import argparse
+    import json
+    args = argparse.Namespace(width=256, height=160, steps=3, warmup=1)
+    bench.run_reference(args, 1, 0, budget_s=1e-6)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["steps"] == 3 and line["value"] > 0
+    assert "band" in line["cpu_baseline"]["sample"] and "256x64" in line["cpu_baseline"]["sample"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] == "port"
+    bench.run_reference(args, 1, 0, budget_s=1e6)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["cpu_baseline"]["sample"].startswith("3 full 256x160 timesteps")
