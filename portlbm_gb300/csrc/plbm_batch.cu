@@ -83,7 +83,9 @@ __global__ void __launch_bounds__(256, PREC == F64_Q60 ? 3 : 6) k_batch(BatchArg
 }
 
 // 2-byte storage: the same queue, each warp updating 256-node row segments with the vectorised
-// row update of k_nptl_vec (blockDim.x == 32; a tile is 256 x (tile_h * tile_rows) nodes).
+// row update of k_nptl_vec (blockDim.x == 32; a tile is 256 x (tile_h * tile_rows) nodes).  The
+// queue loop is repeated rather than shared with k_batch through a tile-body lambda: that version
+// compiled k_batch<F32> with more spilled words and ran 1.8 % slower.
 template <int PREC>
 __global__ void __launch_bounds__(256, 2) k_batch_vec(BatchArgs a)
 {
