@@ -606,8 +606,6 @@ struct plbm_handler {
         cuda_check(cudaMemcpyAsync(flags_d, flags_src, nres, cudaMemcpyHostToDevice, stream), "H2D flags");
         if (has_mask) cuda_check(plbm::launch_check_mask(flags_d, nres, status_d, stream), "mask check");
         cuda_check(plbm::launch_links(flags_d, links, W, H, P, stream), "links kernel");
-        if (opt.gather < PLBM_GATHER_AUTO || opt.gather > PLBM_GATHER_POROUS)
-            fail(PLBM_ERR_ARGUMENT, "gather must be PLBM_GATHER_AUTO, PLBM_GATHER_OPEN or PLBM_GATHER_POROUS");
         // only the shifted forms of nptl/lptl have a porous instantiation
         const bool has_porous = alg <= 1 && (prec == PLBM_F32 || prec == PLBM_F16S || prec == PLBM_BF16S);
         const bool count_obstacles = has_porous && opt.gather == PLBM_GATHER_AUTO;
@@ -964,6 +962,11 @@ static int create_common(plbm_handler *h, const plbm_options *opt, plbm_handler 
 {
     if (opt) h->opt = *opt;
     else plbm_default_options(&h->opt);
+    if (h->opt.gather < PLBM_GATHER_AUTO || h->opt.gather > PLBM_GATHER_POROUS) {
+        set_err(nullptr, Status{ PLBM_ERR_ARGUMENT, "gather must be PLBM_GATHER_AUTO, PLBM_GATHER_OPEN or PLBM_GATHER_POROUS" });
+        delete h;
+        return PLBM_ERR_ARGUMENT;
+    }
     // A settings file's "gb300" object chooses the precision unless the caller's options name
     // one other than the drop-in default.
     h->opt_precision_set = opt && (!h->from_json || opt->precision != PLBM_F64_STRICT);

@@ -175,6 +175,20 @@ def test_flags_match_oracle(plbm, oracle_mod, sc):
 
 
 @pytest.mark.skipif(gpu_available(), reason="checks the failure mode without a GPU")
+def test_invalid_gather_option_is_rejected_before_any_device_work(plbm):
+    import ctypes
+    lib = plbm.load_library()
+    opts = plbm._COpts()
+    lib.plbm_default_options(ctypes.byref(opts))
+    assert opts.gather == plbm.GATHER["auto"]
+    opts.gather = 7
+    c = P(plbm)._c()
+    out = ctypes.c_void_p()
+    rc = lib.plbm_create(ctypes.byref(c), ctypes.byref(opts), ctypes.byref(out))
+    assert rc == -7 and not out.value   # PLBM_ERR_ARGUMENT
+    assert "gather" in lib.plbm_last_error(None).decode()
+
+
 def test_create_without_gpu_fails_loudly(plbm):
     with pytest.raises(plbm.NoDeviceException):
         plbm.create_handler(P(plbm))
