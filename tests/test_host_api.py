@@ -194,6 +194,15 @@ def test_create_without_gpu_fails_loudly(plbm):
         plbm.create_handler(P(plbm))
 
 
+@pytest.mark.skipif(gpu_available(), reason="checks the failure mode without a GPU")
+def test_batch_without_gpu_fails_loudly(plbm):
+    dom = {"mask": plbm.porous_disks(64, 32, 1, 0.8), "relaxation_time": 0.6, "inlet_density": 1.01}
+    with pytest.raises(plbm.NoDeviceException):
+        plbm.Batch([dom], precision="f16s")
+    with pytest.raises(plbm.Exception, match="no domains"):
+        plbm.Batch([], precision="f32")
+
+
 def test_porous_disks_generator(plbm):
     m = plbm.porous_disks(300, 120, 5, 0.7)
     assert m.shape == (120, 300)

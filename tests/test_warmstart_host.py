@@ -87,3 +87,22 @@ def test_state_difference_over_fluid_nodes():
     a = (np.array([1.0, 9.0, 1.0]), np.zeros(3))
     b = (np.array([1.0, -5.0, 2.0]), np.zeros(3))
     assert np.isclose(ws.state_difference(mask, a, b), 1.0 / np.sqrt(5.0))
+
+
+@pytest.mark.parametrize("h,w", [(256, 256), (256, 1024)])
+def test_tensor_core_dispatch_covers_the_network(plbm, h, w):
+    """Every convolution of the operator runs on tcgen05 except the 4-channel input layer; so does
+    every input gradient except the head's (3 channels in): the host-side dispatch predicate over
+    each layer's resolution and channel counts."""
+    import ctypes
+    lib = plbm.load_library()
+    lib.plbm_nn_conv_on_tensor_cores.argtypes = [ctypes.c_int] * 4
+    tc = lib.plbm_nn_conv_on_tensor_cores
+    layers = [(lvl, ci, co) for lvl in range(5) for ci, co in ws.ENC[2 * lvl:2 * lvl + 2]]
+    layers += [(lvl, ci, co) for k, lvl in enumerate((3, 2, 1, 0)) for ci, co in ws.DEC[2 * k:2 * k + 2]]
+    layers.append((0,) + tuple(ws.HEAD))
+    for lvl, ci, co in layers:
+        hh, ww = h >> lvl, w >> lvl
+        assert tc(hh, ww, ci, co) == (0 if ci == ws.C_IN else 1), (lvl, ci, co)
+        if ci != ws.C_IN:   # the input gradient: the same kernel with channels swapped
+            assert tc(hh, ww, co, ci) == (0 if co == ws.HEAD[1] else 1), (lvl, co, ci)
