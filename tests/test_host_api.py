@@ -189,6 +189,7 @@ def test_invalid_gather_option_is_rejected_before_any_device_work(plbm):
     assert "gather" in lib.plbm_last_error(None).decode()
 
 
+@pytest.mark.skipif(gpu_available(), reason="checks the failure mode without a GPU")
 def test_create_without_gpu_fails_loudly(plbm):
     with pytest.raises(plbm.NoDeviceException):
         plbm.create_handler(P(plbm))
