@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import platform
 import subprocess
 
 import numpy as np
@@ -21,18 +22,28 @@ SCENARIOS = {"Hagen-Poiseuille": 0, "walls": 1, "circle": 2, "square": 3, "wing"
              "skyscraper": 5, "porous": 6, "plate": 7, "custom": 100}
 
 
+# "f64": the reference's double arithmetic, every operation rounded (-ffp-contract=off);
+# "f32": its USE_FLOAT build; "f64_contracted": the same double code with the compiler free to fuse
+# multiply-adds, a legal compilation of the reference that rounds differently (used only to measure
+# how strongly a configuration amplifies rounding differences).
+_LIBS_BY_PRECISION = {"f64": "libplbm_oracle.so", "f32": "libplbm_oracle_f32.so",
+                      "f64_contracted": "libplbm_oracle_contracted.so"}
+
+
 def lib_path(precision: str = "f64") -> str:
-    return os.path.join(HERE, "libplbm_oracle.so" if precision == "f64" else "libplbm_oracle_f32.so")
+    return os.path.join(HERE, _LIBS_BY_PRECISION[precision])
 
 
 def build(force: bool = False) -> None:
-    """Compiles the oracle (double and USE_FLOAT variants) with -ffp-contract=off."""
+    """Compiles the oracle variants (see _LIBS_BY_PRECISION)."""
     src = os.path.join(HERE, "plbm_oracle.c")
-    for prec, extra in (("f64", []), ("f32", ["-DPLBMO_FLOAT"])):
+    fma = ["-mfma"] if platform.machine() in ("x86_64", "AMD64") else []
+    for prec, extra in (("f64", ["-ffp-contract=off"]), ("f32", ["-ffp-contract=off", "-DPLBMO_FLOAT"]),
+                        ("f64_contracted", ["-ffp-contract=fast", *fma])):
         out = lib_path(prec)
         if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
             continue
-        cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
+        cmd = ["gcc", "-O2", "-std=c11", "-fno-fast-math", "-fopenmp",
                "-fPIC", "-shared", *extra, "-o", out + ".tmp", src, "-lm"]
         subprocess.run(cmd, check=True)
         os.replace(out + ".tmp", out)
