@@ -2,7 +2,10 @@
 //
 // Mirrors (SC-SGS/PortLBM, paths relative to that project):
 //   lbm::core::Properties                       include/lbm/core/properties.hpp:30-166
-//   lbm::execution::AlgorithmHandler            include/lbm/execution/algorithm_handler.hpp:40-156
+//   lbm::core::Domain                           include/lbm/core/domain.hpp:29-85
+//   lbm::execution::AlgorithmHandler (abstract) include/lbm/execution/algorithm_handler.hpp:40-156
+//   lbm::execution::CUDAAlgorithmHandler        the concrete handler, in the place of
+//                                               include/lbm/execution/sycl_algorithm_handler.hpp:45-455
 //   lbm::create_handler(Properties / path)      include/lbm/portlbm_factory.hpp:59,73
 //   lbm::exceptions::{Exception, json::PropertyArgumentException, algorithm::WaitException}
 //                                               include/lbm/exceptions/exceptions.hpp:31-150
@@ -116,6 +119,16 @@ struct Properties {
         return c;
     }
 
+    // The inverse of to_c(): the C struct carries inner extents, as the constructor takes them.
+    static Properties from_c(const plbm_properties &c)
+    {
+        return Properties(c.algorithm ? c.algorithm : "", c.data_layout ? c.data_layout : "", c.debug_mode != 0,
+                          c.work_group_size, c.time_steps, c.frame_update_interval, c.scenario ? c.scenario : "",
+                          c.vertical_nodes, c.horizontal_nodes, (real_type)c.inlet_velocity_x,
+                          (real_type)c.inlet_velocity_y, (real_type)c.inlet_density, (real_type)c.outlet_velocity_x,
+                          (real_type)c.outlet_velocity_y, (real_type)c.outlet_density, (real_type)c.relaxation_time);
+    }
+
     // Properties::validate (src/lbm/core/simulation.cpp:60-125).
     void validate() const
     {
@@ -124,29 +137,113 @@ struct Properties {
     }
 };
 
+// core::Domain (include/lbm/core/domain.hpp:29-85): the padded / buffered extents and the
+// subdomain (work-group tile) decomposition of one algorithm, computed as
+// src/lbm/core/simulation.cpp:194-382 does.
+class Domain {
+  public:
+    unsigned int total_node_count = 0;
+    unsigned int horizontal_nodes = 0;
+    unsigned int vertical_nodes = 0;
+    unsigned int subdomain_vertical_nodes = 0;
+    unsigned int subdomain_horizontal_nodes = 0;
+    unsigned int subdomain_count_vertical = 0;
+    unsigned int subdomain_count_horizontal = 0;
+
+    Domain() = default;
+    // Domain(Properties&): throws PropertyArgumentException where the reference's swap set-up
+    // rejects the work-group size (below 6).  The library does that settings.json rewrite when a
+    // handler is created from the file; this constructor leaves the file alone.
+    explicit Domain(Properties &properties)
+    {
+        const plbm_properties c = properties.to_c();
+        unsigned v[7] = { 0, 0, 0, 0, 0, 0, 0 };
+        detail::check(plbm_compute_domain(&c, v), nullptr);
+        *this = Domain(v);
+    }
+    // From the seven values plbm_compute_domain / plbm_get_domain write, in the field order above.
+    explicit Domain(const unsigned (&v)[7])
+        : total_node_count(v[0]), horizontal_nodes(v[1]), vertical_nodes(v[2]), subdomain_vertical_nodes(v[3]),
+          subdomain_horizontal_nodes(v[4]), subdomain_count_vertical(v[5]), subdomain_count_horizontal(v[6])
+    {
+    }
+};
+
 }  // namespace core
 
 namespace execution {
 
+// The abstract handler interface (algorithm_handler.hpp:40-156): callers hold a
+// std::unique_ptr<AlgorithmHandler> from lbm::create_handler and use only these members.
 class AlgorithmHandler {
   public:
-    size_t processing_element_constraint = 1024;
+    // Upper bound on the processing elements (threads) per work-group; the concrete handler sets
+    // the device's maximum, as the reference does (sycl_algorithm_handler.hpp:302).
+    size_t processing_element_constraint;
 
-    explicit AlgorithmHandler(plbm_handler *h) : h_(h) { sync(); }
-    ~AlgorithmHandler() { plbm_destroy(h_); }
-    AlgorithmHandler(const AlgorithmHandler &) = delete;
-    AlgorithmHandler &operator=(const AlgorithmHandler &) = delete;
+    virtual ~AlgorithmHandler() = default;
 
-    void initialize() { detail::check(plbm_initialize(h_), h_); }
-    void start() { detail::check(plbm_start(h_), h_); }
-    void pause() { detail::check(plbm_pause(h_), h_); }
-    bool is_finished() const
+    virtual void initialize() = 0;
+    virtual void start() = 0;
+    virtual void pause() = 0;
+    virtual bool is_finished() const = 0;
+    virtual void block_until_finished() = 0;
+
+    virtual std::vector<real_type> &get_densities() const = 0;
+    virtual std::vector<real_type> &get_x_velocities() const = 0;
+    virtual std::vector<real_type> &get_y_velocities() const = 0;
+    virtual std::vector<real_type> &get_absolute_velocities() const = 0;
+
+    // stored extents of the unexpanded domain (inner + 2 ghost layers)
+    virtual unsigned int get_horizontal_nodes() const = 0;
+    virtual unsigned int get_vertical_nodes() const = 0;
+    virtual real_type get_inlet_density() const = 0;
+    virtual real_type get_outlet_density() const = 0;
+    virtual real_type get_progress() const = 0;
+    virtual real_type get_last_frametime() const = 0;
+    virtual unsigned int get_current_iteration() const = 0;
+
+    virtual const core::Properties &get_properties() const = 0;
+    virtual const core::Domain &get_domain() const = 0;
+
+  protected:
+    explicit AlgorithmHandler(size_t constraint) : processing_element_constraint(constraint) {}
+};
+
+// The CUDA implementation behind lbm::create_handler (the counterpart of SYCLAlgorithmHandler,
+// sycl_algorithm_handler.hpp:45-455): owns one libplbm handle.
+class CUDAAlgorithmHandler final : public AlgorithmHandler {
+  public:
+    // every CUDA device's maxThreadsPerBlock
+    static constexpr size_t max_work_group_size = 1024;
+
+    explicit CUDAAlgorithmHandler(plbm_handler *h, std::string settings_path = std::string())
+        : AlgorithmHandler(max_work_group_size), h_(h), settings_path_(std::move(settings_path))
+    {
+        refresh_description();
+        sync();
+    }
+    ~CUDAAlgorithmHandler() override { plbm_destroy(h_); }
+    CUDAAlgorithmHandler(const CUDAAlgorithmHandler &) = delete;
+    CUDAAlgorithmHandler &operator=(const CUDAAlgorithmHandler &) = delete;
+
+    // Rebuilds the simulation; a handler made from settings.json re-reads it, so the properties
+    // and the domain are taken afresh.
+    void initialize() override
+    {
+        detail::check(plbm_initialize(h_), h_);
+        refresh_description();
+        sync();
+    }
+    void start() override { detail::check(plbm_start(h_), h_); }
+    void pause() override { detail::check(plbm_pause(h_), h_); }
+    bool is_finished() const override
     {
         int f = 0;
         plbm_is_finished(h_, &f);
         return f != 0;
     }
-    void block_until_finished()
+    void block_until_finished() override
     {
         detail::check(plbm_block_until_finished(h_), h_);
         sync();
@@ -154,55 +251,66 @@ class AlgorithmHandler {
 
     // The reference returns references to host vectors that the worker thread refreshes on frame
     // steps; these vectors are refreshed from the library's host arrays when a call returns.
-    std::vector<real_type> &get_densities() const { return pull(PLBM_DENSITY); }
-    std::vector<real_type> &get_x_velocities() const { return pull(PLBM_X_VELOCITY); }
-    std::vector<real_type> &get_y_velocities() const { return pull(PLBM_Y_VELOCITY); }
-    std::vector<real_type> &get_absolute_velocities() const { return pull(PLBM_ABS_VELOCITY); }
+    std::vector<real_type> &get_densities() const override { return pull(PLBM_DENSITY); }
+    std::vector<real_type> &get_x_velocities() const override { return pull(PLBM_X_VELOCITY); }
+    std::vector<real_type> &get_y_velocities() const override { return pull(PLBM_Y_VELOCITY); }
+    std::vector<real_type> &get_absolute_velocities() const override { return pull(PLBM_ABS_VELOCITY); }
 
-    unsigned int get_horizontal_nodes() const
+    unsigned int get_horizontal_nodes() const override
     {
         unsigned hn = 0, vn = 0;
         plbm_get_extents(h_, &hn, &vn);
         return hn;
     }
-    unsigned int get_vertical_nodes() const
+    unsigned int get_vertical_nodes() const override
     {
         unsigned hn = 0, vn = 0;
         plbm_get_extents(h_, &hn, &vn);
         return vn;
     }
-    real_type get_inlet_density() const { return props().inlet_density; }
-    real_type get_outlet_density() const { return props().outlet_density; }
-    real_type get_progress() const
+    real_type get_inlet_density() const override { return props_->inlet_density; }
+    real_type get_outlet_density() const override { return props_->outlet_density; }
+    real_type get_progress() const override
     {
         double p = 0;
         plbm_get_progress(h_, &p);
         return (real_type)p;
     }
-    real_type get_last_frametime() const
+    real_type get_last_frametime() const override
     {
         double ms = 0;
         plbm_get_last_frametime(h_, &ms);
         return (real_type)ms;
     }
-    unsigned int get_current_iteration() const
+    unsigned int get_current_iteration() const override
     {
         unsigned it = 0;
         plbm_get_current_iteration(h_, &it);
         return it;
     }
-    plbm_properties props() const
-    {
-        plbm_properties c{};
-        plbm_get_properties(h_, &c);
-        return c;
-    }
+    const core::Properties &get_properties() const override { return *props_; }
+    const core::Domain &get_domain() const override { return dom_; }
+
+    // The C ABI handle, for the measurement and batch entry points of plbm_c.h.
     plbm_handler *native() const { return h_; }
 
   private:
     plbm_handler *h_;
+    std::string settings_path_;
+    std::unique_ptr<core::Properties> props_;
+    core::Domain dom_;
     mutable std::vector<real_type> res_[4];
 
+    void refresh_description()
+    {
+        plbm_properties c{};
+        plbm_get_properties(h_, &c);
+        props_ = std::make_unique<core::Properties>(core::Properties::from_c(c));
+        props_->settings_path = settings_path_;
+        unsigned v[7] = { 0, 0, 0, 0, 0, 0, 0 };
+        plbm_get_domain(h_, v);
+        dom_ = core::Domain(v);
+    }
     std::vector<real_type> &pull(int which) const
     {
         const double *d = nullptr;
@@ -226,7 +334,7 @@ inline std::unique_ptr<execution::AlgorithmHandler> create_handler(const core::P
     const plbm_properties c = props.to_c();
     plbm_handler *h = nullptr;
     detail::check(plbm_create(&c, options, &h), nullptr);
-    return std::make_unique<execution::AlgorithmHandler>(h);
+    return std::make_unique<execution::CUDAAlgorithmHandler>(h, props.settings_path);
 }
 
 inline std::unique_ptr<execution::AlgorithmHandler> create_handler(const std::string &settings_path,
@@ -234,7 +342,7 @@ inline std::unique_ptr<execution::AlgorithmHandler> create_handler(const std::st
 {
     plbm_handler *h = nullptr;
     detail::check(plbm_create_from_json(settings_path.c_str(), options, &h), nullptr);
-    return std::make_unique<execution::AlgorithmHandler>(h);
+    return std::make_unique<execution::CUDAAlgorithmHandler>(h, settings_path);
 }
 
 }  // namespace lbm

@@ -3,12 +3,15 @@
 //   regression tests/test_regression.cpp:67-181 (lptl + stream Hagen-Poiseuille 30x14, tau 1.0,
 //              rho 1.01 / 1.0, 8000 steps: parabolic profile checks)
 //   errors     validate() / unknown algorithm / block_until_finished twice
+//   interface  get_properties() / get_domain() through std::unique_ptr<AlgorithmHandler>
+//              (algorithm_handler.hpp:146,151), checked against core::Domain(Properties&)
 // Exit status 0 when every check holds.
 #include "portlbm_gb300.hpp"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <memory>
 #include <numeric>
 
 static int failures = 0;
@@ -90,8 +93,37 @@ static void errors()
     CHECK(handler->is_finished() && handler->get_current_iteration() == 10);
 }
 
+static void interface()
+{
+    const char *algs[4] = { "nptl", "lptl", "npol", "nsol" };
+    for (const char *alg : algs) {
+        lbm::core::Properties props(alg, "bundle", false, 64, 20, 20, "circle", 37, 91, 0.0, 0.0, 1.05, 0.0, 0.0, 1.0,
+                                    0.7);
+        std::unique_ptr<lbm::execution::AlgorithmHandler> handler = lbm::create_handler(props);
+        const lbm::core::Properties &got = handler->get_properties();
+        CHECK(got.algorithm == alg && got.data_layout == "bundle" && got.scenario == "circle");
+        CHECK(got.vertical_nodes == 39 && got.horizontal_nodes == 93 && got.domain_node_count == 37u * 91u);
+        CHECK(got.work_group_size == 64 && got.time_steps == 20 && got.relaxation_time == 0.7);
+        CHECK(got.inlet_density == 1.05 && got.outlet_density == 1.0);
+        const lbm::core::Domain &dom = handler->get_domain();
+        const lbm::core::Domain want(props);
+        CHECK(dom.total_node_count == want.total_node_count && dom.horizontal_nodes == want.horizontal_nodes &&
+              dom.vertical_nodes == want.vertical_nodes);
+        CHECK(dom.subdomain_vertical_nodes == want.subdomain_vertical_nodes &&
+              dom.subdomain_horizontal_nodes == want.subdomain_horizontal_nodes &&
+              dom.subdomain_count_vertical == want.subdomain_count_vertical &&
+              dom.subdomain_count_horizontal == want.subdomain_count_horizontal);
+        CHECK(dom.total_node_count >= 39u * 93u);
+        CHECK(handler->processing_element_constraint == 1024);
+        handler->start();
+        handler->block_until_finished();
+        CHECK(handler->get_current_iteration() == 20 && handler->get_densities().size() == 37u * 91u);
+    }
+}
+
 int main()
 {
+    interface();
     smoke();
     regression();
     errors();
