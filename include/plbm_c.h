@@ -202,7 +202,9 @@ int plbm_mass_momentum(plbm_handler *h, double out3[3]);
  * every GPU loading the library holds until exit, so inner_h is limited to PLBM_NOALLOC_MAX_ROWS
  * and larger domains are rejected with PLBM_ERR_ARGUMENT.
  *   lattice0/1  device, 9 * P * inner_h doubles each, P = inner_w rounded up to a multiple of 32
- *   flags       device, inner_w * inner_h int8, row-major from (x=1, y=1): 0 fluid, 1 solid
+ *   flags       device, inner_w * inner_h int8, row-major from (x=1, y=1): 0 fluid, 1 solid.  Values
+ *               are not checked (that would need a synchronising read-back): any value other than 0
+ *               acts as solid, both for the node and as a bounce-back source of its neighbours
  *   results     device, 4 * inner_w * inner_h doubles: rho | jx | jy | |j|, written on the last
  *               step of the call
  * first_step == 0 starts a run: it fills both lattices with the rest state, the results with
@@ -212,7 +214,9 @@ int plbm_mass_momentum(plbm_handler *h, double out3[3]);
  * GPU (other streams or threads, or two runs interleaved) race on it.  The first call on each
  * device fetches the array's device address (with that device current); make that first call
  * before any stream capture.  Work is queued on `stream` (a cudaStream_t; NULL = legacy default
- * stream) and not synchronised. */
+ * stream) and not synchronised.  inner_w is limited to 2^30.  A CUDA error already pending on the
+ * calling thread when the call starts is returned as PLBM_ERR_CUDA, named in the message and left
+ * pending (not cleared). */
 #define PLBM_NOALLOC_MAX_ROWS 65536
 typedef struct {
     void *lattice0, *lattice1;

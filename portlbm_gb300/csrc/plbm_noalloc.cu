@@ -20,6 +20,8 @@ namespace {
 
 constexpr unsigned NOALLOC_MAX_ROWS = PLBM_NOALLOC_MAX_ROWS;
 constexpr int NOALLOC_MAX_DEVICES = 64;
+// widest accepted row: the row pitch (inner_w rounded up to 32) and the grid stay within int
+constexpr unsigned NOALLOC_MAX_WIDTH = 1u << 30;
 
 // The scratch: jy at x' = W-2 for two step parities.  Every GPU that loads the library holds it
 // (1 MiB) until the process exits; all calls share it.
@@ -29,7 +31,9 @@ std::mutex g_mu;
 double *g_scratch_addr[NOALLOC_MAX_DEVICES] = {};
 thread_local char g_err[256];
 
-// Solid-source bits are derived from the caller's flag grid on the fly (no link array).
+// Solid-source bits are derived from the caller's flag grid on the fly (no link array).  One rule
+// for both uses of a flag: 0 is fluid, any other value solid (a node that does not update is also
+// a bounce-back source for its neighbours).
 __global__ void k_nptl_noalloc(plbm::StepParams p, const int8_t *flags)
 {
     using namespace plbm;
@@ -42,7 +46,7 @@ __global__ void k_nptl_noalloc(plbm::StepParams p, const int8_t *flags)
     for (int d = 0; d < 9; ++d) {
         if (d == 4) continue;
         const int sx = xi - cxd(d), sy = yi - cyd(d);
-        if (sx >= 0 && sx < p.W && sy >= 0 && sy < p.H && flags[(size_t)sy * p.W + sx] == 1) lk |= (uint16_t)(1u << d);
+        if (sx >= 0 && sx < p.W && sy >= 0 && sy < p.H && flags[(size_t)sy * p.W + sx] != 0) lk |= (uint16_t)(1u << d);
     }
     const unsigned long long n = (unsigned long long)xi + (unsigned long long)yi * p.P;
     double f[9];
@@ -87,6 +91,19 @@ extern "C" int plbm_nptl_steps_noalloc(const plbm_noalloc_args *a)
     if (a->inner_w < 2 || a->inner_h < 2) return fail(PLBM_ERR_ARGUMENT, "plbm_nptl_steps_noalloc: inner extents must be >= 2");
     if (a->inner_h > NOALLOC_MAX_ROWS)
         return fail(PLBM_ERR_ARGUMENT, "plbm_nptl_steps_noalloc: inner_h exceeds PLBM_NOALLOC_MAX_ROWS (65536)");
+    if (a->inner_w > NOALLOC_MAX_WIDTH)
+        return fail(PLBM_ERR_ARGUMENT, "plbm_nptl_steps_noalloc: inner_w exceeds 2^30 nodes");
+    {
+        // an error left pending by the caller's own earlier work is reported, not consumed: the
+        // launch check below would otherwise return (and clear) it as this call's failure
+        const cudaError_t pending = cudaPeekAtLastError();
+        if (pending != cudaSuccess) {
+            char msg[200];
+            std::snprintf(msg, sizeof msg, "plbm_nptl_steps_noalloc: a CUDA error was already pending before the "
+                                           "call (not cleared): %s", cudaGetErrorString(pending));
+            return fail(PLBM_ERR_CUDA, msg);
+        }
+    }
     if (!(a->relaxation_time > 0)) return fail(PLBM_ERR_PROPERTY, "relaxation_time must be > 0");
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES)
