@@ -39,8 +39,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 W_DEFAULT, H_DEFAULT = 8192, 8192
+VARIANT_STEPS = 200          # device-resident steps per storage form in `variants`
+ERR_HEADLINE_STEPS = 50      # steps of the headline channel compared with the CPU oracle
 BYTES_PER_NODE = {"f64_strict": 144.0, "f64_fast": 144.0, "f64_q60": 144.0, "f32_ref": 72.0, "f32": 72.0,
-                  "f16s": 36.0, "bf16s": 36.0}
+                  "f16s": 36.0, "bf16s": 36.0, "f16c": 36.0}
 
 
 def circle_channel_mask(w: int, h: int) -> np.ndarray:
@@ -187,21 +189,57 @@ def cpu_oracle_sample(w, h, steps, mask, threads=None):
     return w * h * steps / dt / 1e6, plbm_oracle.threads(), dt
 
 
-def err_vs_oracle(plbm, precision, steps=2000, w=400, h=100):
-    """max |GPU - oracle| over rho, jx, jy for the 400x100 Hagen-Poiseuille channel."""
+def err_vs_oracle(plbm, precision, steps=2000, w=400, h=100, mask=None, alg="nptl", lay="stream", tau=0.6):
+    """max |GPU - oracle| over rho, jx, jy after `steps` steps: by default the 400x100
+    Hagen-Poiseuille channel; with `mask`, that channel (e.g. the headline circle channel)."""
     from oracle import plbm_oracle
     plbm_oracle.build()
-    props = plbm.Properties("nptl", "stream", False, 1024, steps, steps, "Hagen-Poiseuille", h, w, 0.0, 0.0, 1.2,
-                            0.0, 0.0, 1.0, 0.6)
-    hd = plbm.create_handler(props, precision=precision)
+    props = plbm.Properties(alg, lay, False, 1024, steps, steps, "Hagen-Poiseuille", h, w, 0.0, 0.0, 1.2,
+                            0.0, 0.0, 1.0, tau)
+    hd = plbm.create_handler(props, precision=precision, mask=mask)
     hd.start()
     hd.block_until_finished()
     got = [hd.get_densities(), hd.get_x_velocities(), hd.get_y_velocities()]
     hd.close()
-    o = plbm_oracle.Oracle("nptl", "stream", 1024, "Hagen-Poiseuille", w, h, inlet_density=1.2, relaxation_time=0.6)
+    o = plbm_oracle.Oracle(alg, "stream", 1024, "Hagen-Poiseuille", w, h, inlet_density=1.2, relaxation_time=tau,
+                           mask=mask)
     o.run(steps)
-    ref = [o.result(0), o.result(1), o.result(2)]
-    return float(max(np.max(np.abs(a - b)) for a, b in zip(got, ref)))
+    err = 0.0
+    for i, a in enumerate(got):
+        err = max(err, float(np.max(np.abs(a - o.result(i)))))
+    return err
+
+
+def parity_drift(plbm, w=2000, h=500, checkpoints=(1000, 2000, 5000, 10000), taus=(0.55, 0.6, 1.0),
+                 precisions=("f64_q60", "f64_fast")):
+    """Growth of the FP64-accuracy forms' error against the oracle with the number of steps on the
+    2000x500 circle channel (nptl, stream): max |GPU - oracle| over rho, jx, jy at each checkpoint,
+    GPU handlers and the oracle advanced side by side."""
+    from oracle import plbm_oracle
+    plbm_oracle.build()
+    mask = circle_channel_mask(w, h)
+    out = {"domain": f"{w}x{h} circle channel, nptl+stream, rho 1.2/1.0", "rows": []}
+    for tau in taus:
+        o = plbm_oracle.Oracle("nptl", "stream", 1024, "Hagen-Poiseuille", w, h, inlet_density=1.2,
+                               relaxation_time=tau, mask=mask)
+        props = plbm.Properties("nptl", "stream", False, 1024, 10 ** 8, 10 ** 8, "Hagen-Poiseuille", h, w, 0.0, 0.0,
+                                1.2, 0.0, 0.0, 1.0, tau)
+        hds = {p: plbm.create_handler(props, precision=p, mask=mask) for p in precisions}
+        done = 0
+        for c in checkpoints:
+            o.run(c - done)
+            ref = [o.result(i) for i in range(3)]
+            row = {"tau": tau, "steps": c}
+            for p, hd in hds.items():
+                hd.run_steps(c - done)
+                hd.sync_results()
+                got = [hd.get_densities(), hd.get_x_velocities(), hd.get_y_velocities()]
+                row[p] = max(float(np.max(np.abs(a - b))) for a, b in zip(got, ref))
+            done = c
+            out["rows"].append(row)
+        for hd in hds.values():
+            hd.close()
+    return out
 
 
 # DRAM read + write bytes of one step launch, from ncu captures of the 4096^2 circle channel
@@ -210,23 +248,27 @@ TRAFFIC_PER_NODE = {"nptl_stream_f64_q60": 2.293e9 / (4096 * 4096), "nptl_stream
                     "nptl_stream_f32": 1.1375e9 / (4096 * 4096), "nptl_stream_f16s": 0.5923e9 / (4096 * 4096)}
 
 
-def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, max_steps=100000,
-                    big=(8192, 8192), big_steps=2000, big_cap=None, small=True):
-    """Each storage form against the FP64 drop-in on a seeded porous channel (disks r in [3, 12],
-    tau 0.6, rho 1.01 / 1.0): steps to residual `target`, relative L2 error of the momentum field
-    and relative total-mass difference at steady state; then the same errors on the 8192^2 porous
-    channel against f64_q60 (FP64 accuracy, <= 1e-12 from the drop-in), after `big_steps` steps or,
-    with `big_cap`, run to `target` with at most `big_cap` steps (steps and residual recorded)."""
+def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, max_steps=200000,
+                    ref_target=1e-9, ref_cap=400000, big=(8192, 8192), big_steps=2000, big_cap=None, small=True,
+                    forms=("f64_strict", "f64_fast", "f32", "f16s", "f16c", "bf16s")):
+    """Each storage form against the FP64 steady state on a seeded porous channel (disks r in [3, 12],
+    tau 0.6, rho 1.01 / 1.0).  The reference steady state is f64_q60 (FP64 accuracy, <= 1e-12 from
+    the drop-in) run to residual `ref_target`; every form runs to residual `target` (at most
+    `max_steps` steps) and reports its steps, final residual, relative L2 error of the momentum
+    field and relative total-mass difference against that reference.  (A reference stopped at the
+    forms' own target would still be ~1e-3 away from its steady state and would charge its own
+    transient to the forms.)  Then the same errors on the 8192^2 porous channel against f64_q60,
+    after `big_steps` steps or, with `big_cap`, run to `target` with at most `big_cap` steps."""
     mask = plbm.porous_disks(w, h, seed, porosity)
     fluid = mask.reshape(-1) == 0
 
-    def run(prec, mk, ww, hh, to_residual=True, steps=0, cap=max_steps):
+    def run(prec, mk, ww, hh, to_residual=True, steps=0, cap=max_steps, tgt=target):
         props = plbm.Properties("nptl", "stream", False, 1024, 10 ** 9, 10 ** 9, "Hagen-Poiseuille", hh, ww, 0.0,
                                 0.0, 1.01, 0.0, 0.0, 1.0, 0.6)
         hd = plbm.create_handler(props, precision=prec, mask=mk)
         t0 = time.perf_counter()
         if to_residual:
-            n, r = hd.run_to_residual(target, 100, cap)
+            n, r = hd.run_to_residual(tgt, 100, cap)
         else:
             hd.run_steps(steps)
             hd.sync_results()
@@ -244,10 +286,11 @@ def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, 
 
     study = {"target_residual": target}
     if small:
-        n64, r64, t64, ref = run("f64_strict", mask, w, h)
+        nref, rref, tref, ref = run("f64_q60", mask, w, h, cap=ref_cap, tgt=ref_target)
         study.update({"domain": f"{w}x{h} porous (seed {seed}, porosity {porosity})",
-                      "f64_strict": {"steps": n64, "residual": r64, "seconds": round(t64, 3)}})
-        for prec in ("f64_q60", "f64_fast", "f32", "f16s", "bf16s"):
+                      "reference": {"precision": "f64_q60", "steps": nref, "residual": rref,
+                                    "seconds": round(tref, 3)}})
+        for prec in forms:
             n, r, dt, out = run(prec, mask, w, h)
             l2, dm = errs(out, ref, fluid)
             study[prec] = {"steps": n, "residual": r, "seconds": round(dt, 3), "rel_l2_j_vs_f64": l2,
@@ -261,7 +304,7 @@ def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, 
                       "f64_q60": {"steps": nref, "residual": rref, "seconds": round(tref, 1)}}
     if not conv:
         study["large"]["domain"] += f", {big_steps} steps"
-    for prec in ("f32", "f16s", "bf16s"):
+    for prec in ("f32", "f16s", "f16c", "bf16s"):
         n, r, dt, out = run(prec, bmask, bw, bh, conv, big_steps, big_cap or 0)
         l2, dm = errs(out, bref, bfl)
         study["large"][prec] = {"steps": n, "residual": r, "seconds": round(dt, 1), "rel_l2_j": l2,
@@ -500,6 +543,8 @@ def main():
     ap.add_argument("--nn-bench", action="store_true", help="only the warm-start operator's kernel timings")
     ap.add_argument("--sweep", action="store_true",
                     help="only the FP64 sweep: 4 algorithms x 3 layouts x tau {0.55, 0.6, 1.0} at 2000x500 and 8192^2")
+    ap.add_argument("--parity-drift", action="store_true",
+                    help="only the error growth of f64_q60 / f64_fast against the oracle (2000x500, up to 10^4 steps)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -510,10 +555,12 @@ def main():
     import portlbm_gb300 as plbm
     from portlbm_gb300 import build as b
     b.build()
-    if args.batch_study_only or args.nn_bench or args.sweep or args.precision_study_large:
+    if args.batch_study_only or args.nn_bench or args.sweep or args.precision_study_large or args.parity_drift:
         if rank == 0:
             if args.sweep:
                 key, res = "sweep", sweep(plbm)
+            elif args.parity_drift:
+                key, res = "parity_drift", parity_drift(plbm)
             elif args.precision_study_large:
                 key, res = "precision_study_large", precision_study(plbm, big_cap=args.precision_study_large,
                                                                     small=False)
@@ -563,18 +610,26 @@ def main():
     e2e_mlups = world * w * h * e2e_steps / (e2e_ms * 1e-3) / 1e6
 
     # -- other forms of the same step (device-resident, same K), reported beside --
+    # Each form is timed over VARIANT_STEPS device-resident steps whatever --steps is, so that the
+    # one observables-writing step that ends a run weighs < 1 % of the window.
     variants = {}
     if not args.no_variants and rank == 0:
-        for prec in ("f64_strict", "f64_fast", "f32", "f16s", "bf16s"):
-            if prec == args.precision:
-                continue
-            vms, vh = device_run(plbm, prec, args.algorithm, args.layout, w, h, mask, max(20, args.steps // 4), 5)
+        for prec in ("f64_q60", "f64_strict", "f64_fast", "f32", "f16s", "f16c", "bf16s"):
+            vms, vh = device_run(plbm, prec, args.algorithm, args.layout, w, h, mask, VARIANT_STEPS, 10)
             vh.close()
             variants[prec] = {"mlups": round(w * h / vms / 1e3, 1), "ms_per_step": round(vms, 4),
+                              "steps": VARIANT_STEPS,
                               "hbm_gbs": round(BYTES_PER_NODE[prec] * w * h / vms / 1e6, 1),
                               "frac_of_hbm": round(BYTES_PER_NODE[prec] * w * h / vms / 1e6 / pk["hbm_gbs"], 4)}
+        variants["ratios"] = {f"{p}_over_{q}": round(variants[p]["mlups"] / variants[q]["mlups"], 3)
+                              for p in ("f16s", "f16c") for q in ("f64_q60", "f64_strict")}
 
-    err = err_vs_oracle(plbm, args.precision) if rank == 0 else None
+    err = None
+    if rank == 0:
+        err = {"poiseuille_400x100_2000_steps": err_vs_oracle(plbm, args.precision),
+               f"circle_{w}x{h}_{ERR_HEADLINE_STEPS}_steps": err_vs_oracle(plbm, args.precision, ERR_HEADLINE_STEPS,
+                                                                           w, h, mask=mask, alg=args.algorithm,
+                                                                           lay=args.layout)}
     study = precision_study(plbm) if (rank == 0 and not args.no_study and not args.no_variants) else None
     batch = batch_study(plbm) if (rank == 0 and not args.no_study and not args.no_variants) else None
 
@@ -601,6 +656,10 @@ def main():
                        "parallelism": f"replicas{world}"},
             "roofline": {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                          "frac": round(achieved_gbs / pk["hbm_gbs"], 4), "traffic": traffic,
+                         # DRAM bytes the launch actually moves (ncu traffic; solid nodes move none)
+                         # over the same live launch time
+                         "dram_frac": (round(traffic / (ms * 1e-3) / 1e9 / pk["hbm_gbs"], 4)
+                                       if traffic else None),
                          "peak_source": pk["source"],
                          "note": ("f64_strict/f64_fast are bound by the FP64 pipe (0.5 T DP instr/s measured); "
                                   "f64_q60 runs the update on the integer pipe")},

@@ -52,9 +52,12 @@ enum { PLBM_DENSITY = 0, PLBM_X_VELOCITY = 1, PLBM_Y_VELOCITY = 2, PLBM_ABS_VELO
  * collide in FP32.  F64_Q60 keeps FP64 accuracy (populations as 64-bit fixed point,
  * round(f * 2^60), finer than an FP64 ulp for |f| >= 2^-7) and collides on the integer pipe,
  * which GB300 issues ~38x faster than FP64; agrees with F64_STRICT to <= 1e-12 and fails with
- * PLBM_ERR_NUMERIC if a population leaves [-4, 4). */
+ * PLBM_ERR_NUMERIC if a population leaves [-4, 4).  F16C stores the same shifted deviations as
+ * F16S in a 16-bit float of 1 sign, 4 exponent and 11 significand bits (the FP16C format of Lehmann
+ * et al., Phys. Rev. E 106, 015308, 2022; half the rounding error of IEEE half) for |f - w rho0|
+ * < 0.5, and fails with PLBM_ERR_NUMERIC when a deviation leaves that range. */
 enum { PLBM_F64_STRICT = 0, PLBM_F64_FAST = 1, PLBM_F32_REF = 2, PLBM_F32 = 3, PLBM_F16S = 4, PLBM_BF16S = 5,
-       PLBM_F64_Q60 = 6 };
+       PLBM_F64_Q60 = 6, PLBM_F16C = 7 };
 
 typedef struct plbm_handler plbm_handler;
 
@@ -78,7 +81,7 @@ typedef struct {
 
 /* Options with no counterpart in the reference; plbm_default_options() gives the drop-in. */
 typedef struct {
-    int precision;          /* PLBM_F64_STRICT ... PLBM_BF16S */
+    int precision;          /* PLBM_F64_STRICT ... PLBM_F16C */
     int nan_protection;     /* WITH_NAN_PROTECTION (CMakeLists.txt:28, default ON) */
     int use_graph;          /* capture chunks of steps in a CUDA graph */
     int device;             /* CUDA device ordinal */
@@ -259,7 +262,7 @@ int plbm_porous_disks(unsigned inner_w, unsigned inner_h, uint64_t seed, double 
  * captured CUDA graph; PLBM_BATCH_PER_DOMAIN launches one kernel per domain per step (the
  * comparison).  Each domain is a channel with its own W x H mask (0 fluid, 1 solid; copied),
  * zero inlet/outlet velocity; nptl update, stream layout.  Precisions: PLBM_F32, PLBM_F16S,
- * PLBM_BF16S, PLBM_F64_Q60. */
+ * PLBM_BF16S, PLBM_F16C, PLBM_F64_Q60. */
 typedef struct plbm_batch plbm_batch;
 typedef struct {
     unsigned inner_w, inner_h;
@@ -273,7 +276,7 @@ void plbm_batch_destroy(plbm_batch *b);
 /* Tile shape and resident blocks per SM of the persistent launch: a block of tile_w x (tile_h & 255)
  * threads, each sweeping rows = ((tile_h >> 8) & 255) rows (at least 1), so a tile covers
  * tile_w x ((tile_h & 255) * rows) nodes.  PLBM_BATCH_TILE_VEC in tile_h selects vectorised rows
- * for PLBM_F16S / PLBM_BF16S batches (8 nodes per thread, one warp per 256-node row segment):
+ * for PLBM_F16S / PLBM_BF16S / PLBM_F16C batches (8 nodes per thread, one warp per 256-node row segment):
  * tile_w must then be 32 and (tile_h & 255) at most 8, and a tile covers
  * 256 x ((tile_h & 255) * rows) nodes. */
 #define PLBM_BATCH_TILE_VEC 0x10000

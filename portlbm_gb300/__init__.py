@@ -31,7 +31,8 @@ __all__ = [
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-PRECISIONS = {"f64_strict": 0, "f64_fast": 1, "f32_ref": 2, "f32": 3, "f16s": 4, "bf16s": 5, "f64_q60": 6}
+PRECISIONS = {"f64_strict": 0, "f64_fast": 1, "f32_ref": 2, "f32": 3, "f16s": 4, "bf16s": 5, "f64_q60": 6,
+              "f16c": 7}
 BYTES_PER_VALUE = {0: 8, 1: 8, 2: 4, 3: 4, 4: 2, 5: 2, 6: 8}
 
 

@@ -18,7 +18,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libplbm.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["k_nptl.cu", "k_lptl.cu", "k_npol.cu", "k_nsol.cu", "plbm_util.cu", "plbm_noalloc.cu", "plbm_batch.cu", "plbm_nn.cu", "plbm_nn_tc.cu"]
+CU_SOURCES = ["k_nptl.cu", "k_lptl.cu", "k_npol.cu", "k_nsol.cu", "k_debug.cu", "plbm_util.cu", "plbm_noalloc.cu", "plbm_batch.cu", "plbm_nn.cu", "plbm_nn_tc.cu"]
 CPP_SOURCES = ["plbm_host.cpp", "plbm_benchmark.cpp"]
 
 

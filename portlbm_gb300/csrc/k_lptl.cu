@@ -5,7 +5,7 @@
 namespace plbm {
 cudaError_t launch_lptl(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s, bool porous)
 {
-    if (porous && prec >= F32 && prec <= BF16S) {
+    if (porous && ((prec >= F32 && prec <= BF16S) || prec == F16C)) {
         switch (prec * 3 + lay) {
             PLBM_POROUS_CASES(k_lptl)
         default: return cudaErrorInvalidValue;

@@ -177,7 +177,7 @@ struct plbm_batch {
     }
 
     unsigned n_domains() const { return (unsigned)(host.size() / 2); }
-    bool two_byte() const { return prec == PLBM_F16S || prec == PLBM_BF16S; }
+    bool two_byte() const { return prec == PLBM_F16S || prec == PLBM_BF16S || prec == PLBM_F16C; }
     // vectorised rows (2-byte storage only): one warp per 256-node row segment
     bool vec_rows = false;
     bool vec() const { return vec_rows; }
@@ -196,8 +196,14 @@ struct plbm_batch {
             for (int k = 0; k < nx * ny; ++k) { dom.push_back(i); loc.push_back((unsigned)k); }
         }
         n_tiles = (unsigned)dom.size();
-        for (unsigned *p : { tile_domain_d, tile_local_d }) if (p) cudaFree(p);
+        // the old arrays may be referenced by the captured graph: drop it first (cudaFree waits for
+        // work in flight), and clear each pointer so a failed allocation leaves none dangling
+        if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+        if (tile_domain_d) cudaFree(tile_domain_d);
+        if (tile_local_d) cudaFree(tile_local_d);
         if (tiles_x_d) cudaFree(tiles_x_d);
+        tile_domain_d = tile_local_d = nullptr;
+        tiles_x_d = nullptr;
         cudaError_t e = cudaMalloc(&tile_domain_d, n_tiles * sizeof(unsigned));
         if (e == cudaSuccess) e = cudaMalloc(&tile_local_d, n_tiles * sizeof(unsigned));
         if (e == cudaSuccess) e = cudaMalloc(&tiles_x_d, tx.size() * sizeof(int));
@@ -231,6 +237,10 @@ struct plbm_batch {
             if (vec()) plbm::k_batch_vec<plbm::BF16S><<<blocks, block, 0, stream>>>(a);
             else plbm::k_batch<plbm::BF16S><<<blocks, block, 0, stream>>>(a);
             break;
+        case PLBM_F16C:
+            if (vec()) plbm::k_batch_vec<plbm::F16C><<<blocks, block, 0, stream>>>(a);
+            else plbm::k_batch<plbm::F16C><<<blocks, block, 0, stream>>>(a);
+            break;
         default: plbm::k_batch<plbm::F64_Q60><<<blocks, block, 0, stream>>>(a); break;
         }
         return cudaGetLastError();
@@ -246,6 +256,7 @@ struct plbm_batch {
             case PLBM_F32: plbm::k_batch_single<plbm::F32><<<grid, block, 0, stream>>>(a, i); break;
             case PLBM_F16S: plbm::k_batch_single<plbm::F16S><<<grid, block, 0, stream>>>(a, i); break;
             case PLBM_BF16S: plbm::k_batch_single<plbm::BF16S><<<grid, block, 0, stream>>>(a, i); break;
+            case PLBM_F16C: plbm::k_batch_single<plbm::F16C><<<grid, block, 0, stream>>>(a, i); break;
             default: plbm::k_batch_single<plbm::F64_Q60><<<grid, block, 0, stream>>>(a, i); break;
             }
         }
@@ -286,8 +297,10 @@ extern "C" {
 int plbm_batch_create(unsigned n, const plbm_batch_domain *doms, int precision, plbm_batch **out)
 {
     if (!doms || !out || n == 0) return berr(nullptr, PLBM_ERR_ARGUMENT, "plbm_batch_create: no domains");
-    if (precision != PLBM_F32 && precision != PLBM_F16S && precision != PLBM_BF16S && precision != PLBM_F64_Q60)
-        return berr(nullptr, PLBM_ERR_ARGUMENT, "batches support PLBM_F32, PLBM_F16S, PLBM_BF16S and PLBM_F64_Q60");
+    if (precision != PLBM_F32 && precision != PLBM_F16S && precision != PLBM_BF16S && precision != PLBM_F64_Q60 &&
+        precision != PLBM_F16C)
+        return berr(nullptr, PLBM_ERR_ARGUMENT,
+                    "batches support PLBM_F32, PLBM_F16S, PLBM_BF16S, PLBM_F16C and PLBM_F64_Q60");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return berr(nullptr, PLBM_ERR_NO_DEVICE, "no CUDA device");
     auto *b = new plbm_batch();
@@ -386,10 +399,12 @@ int plbm_batch_set_tile(plbm_batch *b, int tile_w, int tile_h, int blocks_per_sm
     // tile_h = threads_y + 256 * rows (+ PLBM_BATCH_TILE_VEC)
     const int ty = tile_h & 255, rows = std::max(1, (tile_h >> 8) & 255);
     const bool v = (tile_h & PLBM_BATCH_TILE_VEC) != 0;
-    if (tile_w < 1 || ty < 1 || tile_w * ty > 1024 || blocks_per_sm < 1)
-        return berr(b, PLBM_ERR_ARGUMENT, "tile must have 1..1024 threads");
+    // k_batch / k_batch_vec are compiled for at most 256 threads per block (__launch_bounds__)
+    if (tile_w < 1 || ty < 1 || tile_w * ty > 256 || blocks_per_sm < 1)
+        return berr(b, PLBM_ERR_ARGUMENT, "tile must have 1..256 threads and blocks_per_sm >= 1");
     if (v && (!b->two_byte() || tile_w != 32 || ty > 8))
-        return berr(b, PLBM_ERR_ARGUMENT, "vectorised rows: PLBM_F16S / PLBM_BF16S batches, tiles of 32 x (1..8) threads");
+        return berr(b, PLBM_ERR_ARGUMENT,
+                    "vectorised rows: PLBM_F16S / PLBM_BF16S / PLBM_F16C batches, tiles of 32 x (1..8) threads");
     b->vec_rows = v;
     b->tile_w = tile_w;
     b->tile_h = ty;
@@ -432,7 +447,9 @@ int plbm_batch_run(plbm_batch *b, unsigned steps, int mode, double *ms_per_step)
     if (ms_per_step) *ms_per_step = steps ? ms / steps : 0.0;
     int st = 0;
     cudaMemcpy(&st, b->status_d, sizeof(int), cudaMemcpyDeviceToHost);
-    if (st) return berr(b, PLBM_ERR_NUMERIC, "a population left the f64_q60 range");
+    if (st)
+        return berr(b, PLBM_ERR_NUMERIC, b->prec == PLBM_F16C ? "a population deviation left the f16c range"
+                                                              : "a population left the f64_q60 range");
     return PLBM_OK;
 }
 
@@ -475,7 +492,9 @@ int plbm_batch_results(plbm_batch *b, unsigned domain, int which, double *out)
     if (domain >= b->n_domains() || which < 0 || which > 3) return berr(b, PLBM_ERR_ARGUMENT, "bad domain/which");
     const StepParams &d = b->host[2 * domain];
     const double *src = which == 0 ? d.rho : which == 1 ? d.jx : which == 2 ? d.jy : d.jabs;
-    const cudaError_t e = cudaMemcpy(out, src, (size_t)d.W * d.H * 8, cudaMemcpyDeviceToHost);
+    // on the batch's own (non-blocking) stream, so the copy is ordered after its steps
+    cudaError_t e = cudaMemcpyAsync(out, src, (size_t)d.W * d.H * 8, cudaMemcpyDeviceToHost, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     return e == cudaSuccess ? PLBM_OK : berr(b, PLBM_ERR_CUDA, cudaGetErrorString(e));
 }
 

@@ -85,7 +85,10 @@ class Bench {
         else plbm_default_options(&opts_);
         opts_.mask = nullptr;   // the benchmark runs the scenarios' own geometry
         bytes_node_ = 18.0 * (opts_.precision == PLBM_F32_REF || opts_.precision == PLBM_F32 ? 4
-                              : opts_.precision == PLBM_F16S || opts_.precision == PLBM_BF16S ? 2 : 8);
+                              : opts_.precision == PLBM_F16S || opts_.precision == PLBM_BF16S ||
+                                        opts_.precision == PLBM_F16C
+                                    ? 2
+                                    : 8);
     }
 
     // One run; false if the configuration was rejected (the error is printed).

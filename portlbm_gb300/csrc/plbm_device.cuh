@@ -51,13 +51,33 @@ template <> struct Store<F32> { using T = float; using C = float; };
 template <> struct Store<F16S> { using T = __half; using C = float; };
 template <> struct Store<BF16S> { using T = __nv_bfloat16; using C = float; };
 template <> struct Store<F64_Q60> { using T = long long; using C = long long; };
+template <> struct Store<F16C> { using T = unsigned short; using C = float; };
 
 // The FP32 / FP16 / BF16 forms hold every population as its deviation from rest,
 // df = f - w_d * rho0 (rho0 = 1), in storage AND in the collision: the BGK update is linear in
 // the rest part (feq_d - w_d = w_d (drho + 3 cu + 4.5 cu^2 - 1.5 u^2) with rho = 1 + drho), so the
 // same arithmetic applied to df yields df'.  Rounding then scales with the deviation from rest,
 // not with f itself.
-template <int PREC> __host__ __device__ constexpr bool shifted() { return PREC == F32 || PREC == F16S || PREC == BF16S; }
+template <int PREC> __host__ __device__ constexpr bool shifted()
+{
+    return PREC == F32 || PREC == F16S || PREC == BF16S || PREC == F16C;
+}
+
+// The 16-bit F16C pattern <-> float (see F16C_DECODE in plbm_params.h).  f16c_bits returns the
+// pattern, saturated to the largest magnitude, and sets `over` when |v| >= 0.5 (or v is NaN).
+__device__ __forceinline__ float f16c_value(unsigned u)
+{
+    return __uint_as_float(((u & 0x7FFFu) << 12) | ((u & 0x8000u) << 16)) * F16C_DECODE;
+}
+__device__ __forceinline__ unsigned f16c_bits(float v, bool &over)
+{
+    const unsigned b = __float_as_uint(v * F16C_ENCODE);
+    const unsigned mag = b & 0x7FFFFFFFu;
+    unsigned r = (mag + 0x7FFu + ((mag >> 12) & 1u)) >> 12;
+    over = r > F16C_MAX_BITS;
+    r = over ? F16C_MAX_BITS : r;
+    return r | ((b >> 16) & 0x8000u);
+}
 
 
 template <int PREC>
@@ -68,6 +88,7 @@ __device__ __forceinline__ typename Store<PREC>::C ld(const void *base, unsigned
     (void)d; (void)p;
     if constexpr (PREC == F16S) return __half2float(b[i]);   // df * F16_SCALE, the FP16 form's compute value
     else if constexpr (PREC == BF16S) return __bfloat162float(b[i]);
+    else if constexpr (PREC == F16C) return f16c_value(b[i]);
     else return b[i];
 }
 
@@ -79,7 +100,11 @@ __device__ __forceinline__ void st(void *base, unsigned long long i, int d, type
     (void)d; (void)p;
     if constexpr (PREC == F16S) b[i] = __float2half_rn(v);
     else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(v);
-    else b[i] = v;
+    else if constexpr (PREC == F16C) {
+        bool over;
+        b[i] = (unsigned short)f16c_bits(v, over);
+        if (over) atomicOr(p.status, 1);
+    } else b[i] = v;
 }
 
 // ---- the BGK update ------------------------------------------------------------------------

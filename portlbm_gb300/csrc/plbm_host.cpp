@@ -51,6 +51,21 @@ void cuda_check(cudaError_t e, const char *what)
     if (e != cudaSuccess) fail(PLBM_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+// PLBM_TRACE=1 in the environment: handler set-up and runs print the wall-clock milliseconds of
+// their phases to stderr (observability; off by default).
+struct PhaseTrace {
+    bool on;
+    const char *what;
+    std::chrono::steady_clock::time_point t0;
+    explicit PhaseTrace(const char *w) : on(std::getenv("PLBM_TRACE") != nullptr), what(w), t0(std::chrono::steady_clock::now()) {}
+    void operator()(const char *phase) const
+    {
+        if (!on) return;
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        std::fprintf(stderr, "[plbm] %s %s %.2f ms\n", what, phase, ms);
+    }
+};
+
 // ---- core::Properties (include/lbm/core/properties.hpp:30-166) ---------------------------
 
 struct Props {
@@ -171,11 +186,11 @@ struct JsonExtras {
 
 int precision_from_name(const std::string &s)
 {
-    static const char *names[] = { "f64_strict", "f64_fast", "f32_ref", "f32", "f16s", "bf16s", "f64_q60" };
-    for (int i = 0; i < 7; ++i)
+    static const char *names[] = { "f64_strict", "f64_fast", "f32_ref", "f32", "f16s", "bf16s", "f64_q60", "f16c" };
+    for (int i = 0; i < 8; ++i)
         if (s == names[i]) return i;
-    fail(PLBM_ERR_PROPERTY,
-         "Unknown gb300.precision: \"" + s + "\". Valid values: f64_strict, f64_fast, f32_ref, f32, f16s, bf16s, f64_q60");
+    fail(PLBM_ERR_PROPERTY, "Unknown gb300.precision: \"" + s +
+                                "\". Valid values: f64_strict, f64_fast, f32_ref, f32, f16s, bf16s, f64_q60, f16c");
 }
 
 // json_to_properties(path, offset): the node counts read are inner extents plus `offset`, and the
@@ -397,6 +412,28 @@ std::string g_create_error;
 
 }  // namespace
 
+// Host result arrays: allocation alignment (the largest base page size of the supported hosts).
+static constexpr size_t HOST_ALIGN = 65536;
+
+// Sets the four result arrays to their initial values (rho = -1, j = 0), the pages first touched
+// by up to 16 threads: writing gigabytes of fresh pages is bound by the kernel's page zeroing,
+// which scales with the threads.
+static void parallel_fill(double *const res[4], size_t n)
+{
+    const size_t bytes = 4 * n * sizeof(double);
+    unsigned nt = bytes < (64u << 20) ? 1u : std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+    auto fill = [&](unsigned t) {
+        for (int i = 0; i < 4; ++i) {
+            const size_t a = n * t / nt, b = n * (t + 1) / nt;
+            std::fill(res[i] + a, res[i] + b, i == 0 ? -1.0 : 0.0);
+        }
+    };
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(fill, t);
+    fill(0);
+    for (auto &th : pool) th.join();
+}
+
 // ---- the handler --------------------------------------------------------------------------
 
 struct plbm_handler {
@@ -405,14 +442,20 @@ struct plbm_handler {
     bool from_json = false;
     plbm_options opt{};
     bool opt_precision_set = false;
-    std::vector<int8_t> user_mask;
-    const int8_t *mask_src = nullptr;   // the caller's mask during plbm_create (uploaded from there)
+    // A caller's mask is uploaded once, from the caller's buffer during plbm_create, into mask_d,
+    // which stays on the device for later initialize() calls (a host copy of an 8192^2 mask would
+    // cost more than the whole device set-up).
+    const int8_t *mask_src = nullptr;   // the caller's mask during plbm_create
+    int8_t *mask_d = nullptr;
+    size_t mask_n = 0;
     bool has_mask = false;
     Domain dom{};
     int alg = 0, lay = 0, prec = 0;
     int W = 0, H = 0, P = 0;
     unsigned long long N = 0;
     int outlet_mode = 0;
+    // debugMode on nptl / lptl: the reference's unfused stream / observables / collide kernels
+    bool debug = false;
     bool porous = false;   // nptl/lptl shifted forms: the obstacle-select gather (PLBM_GATHER_POROUS)
 
     cudaStream_t stream = nullptr;
@@ -429,9 +472,14 @@ struct plbm_handler {
     std::string export_dir;      // frame export (empty: off)
     unsigned export_fields = 0;  // bit i: result i (PLBM_DENSITY ..)
     double *res_h[4] = { nullptr, nullptr, nullptr, nullptr };
-    // The pinned host result arrays are allocated and set to their initial values on a host
-    // thread while the device is already set up and stepping (pinning gigabytes takes a sizeable
-    // fraction of a second); every access waits for it first (wait_host()).
+    double *res_hd[4] = { nullptr, nullptr, nullptr, nullptr };   // device addresses of res_h
+    size_t res_h_bytes = 0;
+    bool res_h_registered = false;
+    // The host result arrays are allocated, first touched with their initial values by parallel
+    // threads and then registered with the driver (page-locked, device-mapped), all on a host
+    // thread while the device is set up and stepping; every access waits for it (wait_host()).
+    // cudaMallocHost would zero and lock the same pages on one thread while holding the driver's
+    // lock, stalling the device set-up behind it (~70 ms for the four 537 MB arrays of 8192^2).
     std::future<std::string> host_ready;
     std::mutex host_mu;            // the step-loop thread and a caller's getter may both wait
     std::string host_err;
@@ -469,7 +517,11 @@ struct plbm_handler {
     std::string worker_error;
     std::string last_error;
 
-    ~plbm_handler() { release(); }
+    ~plbm_handler()
+    {
+        release();
+        if (mask_d) cudaFree(mask_d);
+    }
 
     void release()
     {
@@ -483,7 +535,13 @@ struct plbm_handler {
         for (auto &p : res_d) { if (p) cudaFree(p); p = nullptr; }
         join_host();
         host_err.clear();
-        for (auto &p : res_h) { if (p) cudaFreeHost(p); p = nullptr; }
+        for (int i = 0; i < 4; ++i) {
+            if (res_h[i] && res_h_registered) cudaHostUnregister(res_h[i]);
+            std::free(res_h[i]);
+            res_h[i] = nullptr;
+            res_hd[i] = nullptr;
+        }
+        res_h_registered = false;
         if (links) cudaFree(links);
         if (flags_d) cudaFree(flags_d);
         if (jy_d) cudaFree(jy_d);
@@ -505,6 +563,7 @@ struct plbm_handler {
     // 438-519) + setup_domain (domain_initialization.hpp:453-518).
     void build()
     {
+        const PhaseTrace trace("create");
         release();
         iteration = 0; progress = 0.0; frametime = 1.7976931348623157e308; jprev_iter = -1;
         stop = false; active = false; future_valid = true; worker_status = PLBM_OK; worker_error.clear();
@@ -520,7 +579,13 @@ struct plbm_handler {
         prec = opt.precision;
         if (ex.precision >= 0 && !opt_precision_set) prec = ex.precision;
         if (ex.nan_protection >= 0) opt.nan_protection = ex.nan_protection;
-        if (prec < 0 || prec > 6) fail(PLBM_ERR_ARGUMENT, "precision must be one of PLBM_F64_STRICT..PLBM_F64_Q60");
+        if (prec < 0 || prec > 7) fail(PLBM_ERR_ARGUMENT, "precision must be one of PLBM_F64_STRICT..PLBM_F16C");
+        // NPTLDebug / LPTLDebug run unfused kernels (sycl_algorithm_handler.hpp:164-246); NPOLDebug
+        // and NSOLDebug keep the fused step, as here
+        debug = props.debug_mode && (props.algorithm == "nptl" || props.algorithm == "lptl");
+        if (debug && prec != PLBM_F64_STRICT && prec != PLBM_F32_REF)
+            fail(PLBM_ERR_ARGUMENT, "debugMode runs the reference's unfused kernels, in the f64_strict or f32_ref "
+                                    "form only");
 
         int ndev = 0;
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) fail(PLBM_ERR_NO_DEVICE, "no CUDA device available");
@@ -567,13 +632,14 @@ struct plbm_handler {
         outlet_mode = 0;
         if ((alg == 2 || alg == 3) && ((props.horizontal_nodes - 3) % dom.subdomain_horizontal_nodes) == 0) outlet_mode = 1;
 
-        if (has_mask && user_mask.size() != nres) fail(PLBM_ERR_ARGUMENT, "mask must hold inner W*H entries");
+        if (has_mask && mask_n != nres) fail(PLBM_ERR_ARGUMENT, "mask must hold inner W*H entries");
         // a caller's mask is uploaded as it is (its 0/1 values are checked on the device below);
         // otherwise the scenario's flags are built on the host
         std::vector<int8_t> flags;
         if (!has_mask) flags = make_flags(props, nullptr);
-        const int8_t *flags_src = has_mask ? (mask_src ? mask_src : user_mask.data()) : flags.data();
+        const int8_t *flags_src = has_mask ? mask_d : flags.data();
 
+        trace("host checks");
         cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
         cuda_check(cudaEventCreate(&ev0), "event");
         cuda_check(cudaEventCreate(&ev1), "event");
@@ -589,13 +655,25 @@ struct plbm_handler {
         cuda_check(cudaMalloc(&links, N * sizeof(uint16_t)), "cudaMalloc links");
         cuda_check(cudaMalloc(&flags_d, nres), "cudaMalloc flags");
         for (auto &r : res_d) cuda_check(cudaMalloc(&r, nres * sizeof(double)), "cudaMalloc results");
-        host_ready = std::async(std::launch::async, [this, dev = opt.device]() -> std::string {
-            if (cudaSetDevice(dev) != cudaSuccess) return "cudaSetDevice (host results)";
-            for (auto &r : res_h)
-                if (cudaMallocHost(&r, nres * sizeof(double)) != cudaSuccess) return "cudaMallocHost results";
+        trace("device allocations");
+        host_ready = std::async(std::launch::async, [this, dev = opt.device, trace]() -> std::string {
+            res_h_bytes = (nres * sizeof(double) + HOST_ALIGN - 1) / HOST_ALIGN * HOST_ALIGN;
+            for (auto &r : res_h) {
+                r = static_cast<double *>(std::aligned_alloc(HOST_ALIGN, res_h_bytes));
+                if (!r) return "out of host memory for the results";
+            }
             // initial results: rho = -1, j = 0 (simulation.cpp:386-417)
-            std::fill(res_h[0], res_h[0] + nres, -1.0);
-            for (int i = 1; i < 4; ++i) std::fill(res_h[i], res_h[i] + nres, 0.0);
+            parallel_fill(res_h, nres);
+            trace("host results filled");
+            if (cudaSetDevice(dev) != cudaSuccess) return "cudaSetDevice (host results)";
+            for (int i = 0; i < 4; ++i) {
+                if (cudaHostRegister(res_h[i], res_h_bytes, cudaHostRegisterMapped) != cudaSuccess)
+                    return "cudaHostRegister results";
+                res_h_registered = true;
+                if (cudaHostGetDevicePointer((void **)&res_hd[i], res_h[i], 0) != cudaSuccess)
+                    return "cudaHostGetDevicePointer results";
+            }
+            trace("host results ready");
             return std::string();
         });
         cuda_check(cudaMalloc(&jy_d, 2ull * H * sizeof(double)), "cudaMalloc jy");
@@ -603,16 +681,24 @@ struct plbm_handler {
         cuda_check(cudaMalloc(&red_d, 3 * sizeof(double)), "cudaMalloc reduce");
         cuda_check(cudaMalloc(&status_d, sizeof(int)), "cudaMalloc status");
         cuda_check(cudaMemsetAsync(status_d, 0, sizeof(int), stream), "memset status");
-        cuda_check(cudaMemcpyAsync(flags_d, flags_src, nres, cudaMemcpyHostToDevice, stream), "H2D flags");
+        if (has_mask && !mask_d) {
+            cuda_check(cudaMalloc(&mask_d, mask_n), "cudaMalloc mask");
+            cuda_check(cudaMemcpyAsync(mask_d, mask_src, mask_n, cudaMemcpyHostToDevice, stream), "H2D mask");
+            flags_src = mask_d;
+        }
+        cuda_check(cudaMemcpyAsync(flags_d, flags_src, nres, has_mask ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                   stream), "flags");
         if (has_mask) cuda_check(plbm::launch_check_mask(flags_d, nres, status_d, stream), "mask check");
         cuda_check(plbm::launch_links(flags_d, links, W, H, P, stream), "links kernel");
         // only the shifted forms of nptl/lptl have a porous instantiation
-        const bool has_porous = alg <= 1 && (prec == PLBM_F32 || prec == PLBM_F16S || prec == PLBM_BF16S);
+        const bool has_porous =
+            alg <= 1 && (prec == PLBM_F32 || prec == PLBM_F16S || prec == PLBM_BF16S || prec == PLBM_F16C);
         const bool count_obstacles = has_porous && opt.gather == PLBM_GATHER_AUTO;
         if (count_obstacles)   // read after the initialisation sync below
             cuda_check(plbm::launch_count_obstacle_nodes(links, W, H, P, reinterpret_cast<unsigned long long *>(red_d),
                                                          stream), "obstacle count");
         cuda_check(plbm::launch_fill_results(res_d[0], res_d[1], res_d[2], res_d[3], nres, stream), "results fill");
+        trace("mask upload and geometry kernels queued");
 
         // Ghost constants and rest state in the arithmetic of the chosen form.
         plbm::StepParams &b = base;
@@ -634,7 +720,7 @@ struct plbm_handler {
             b.omega = (double)(1 / (float)props.tau);
             b.rho_out = (double)(float)props.orho;
         }
-        const bool shifted = prec == PLBM_F32 || prec == PLBM_F16S || prec == PLBM_BF16S;
+        const bool shifted = prec == PLBM_F32 || prec == PLBM_F16S || prec == PLBM_BF16S || prec == PLBM_F16C;
         // the shifted forms keep deviations from w_d * rho0(x'): the straight inlet-outlet profile
         // for the two-lattice pull schemes, rho0 = 1 for npol/nsol
         b.W = W;
@@ -643,6 +729,19 @@ struct plbm_handler {
         {
             plbm::fill_q60_constants(b);
             b.status = status_d;
+            if (prec == PLBM_F16C) {
+                // the stored deviations of the boundary constants and of the rest state must fit
+                // the format (|df| < 0.5); a run that leaves the range later sets the status word
+                double worst = 0;
+                for (int d = 0; d < 9; ++d) {
+                    worst = std::max({ worst, std::fabs((double)b.weightf[d]), std::fabs((double)b.feq_inf[d]),
+                                       std::fabs((double)b.feq_outf[d]),
+                                       std::fabs((double)b.weightf[d] + (double)b.shift_wg[d] * (W - 1)) });
+                }
+                if (!(worst < 0.5))
+                    fail(PLBM_ERR_NUMERIC, "f16c stores deviations |f - w rho0| < 0.5; these boundary densities "
+                                           "exceed it (use f32 or f16s)");
+            }
             if (prec == PLBM_F64_Q60) {
                 if (!(props.tau > 0.5))
                     fail(PLBM_ERR_NUMERIC, "f64_q60 needs relaxation_time > 0.5 (omega/2 below 1); use f64_strict");
@@ -705,7 +804,9 @@ struct plbm_handler {
                            "halo fill");
             }
         }
+        trace("initialisation queued");
         cuda_check(cudaStreamSynchronize(stream), "initialisation");
+        trace("initialisation done");
         porous = has_porous && opt.gather == PLBM_GATHER_POROUS;
         if (count_obstacles) {
             unsigned long long c[2] = { 0, 0 };
@@ -717,6 +818,7 @@ struct plbm_handler {
             cuda_check(cudaMemcpy(&bad, status_d, sizeof(int), cudaMemcpyDeviceToHost), "mask check");
             if (bad) fail(PLBM_ERR_ARGUMENT, "mask entries must be 0 (fluid) or 1 (solid)");
         }
+        trace("ready");
     }
 
     // to_host: the step writes its observables straight into the pinned host arrays (device
@@ -726,12 +828,13 @@ struct plbm_handler {
         plbm::StepParams p = base;
         const unsigned par = t & 1u;
         p.write_results = results ? 1 : 0;
-        if (to_host) { p.rho = res_h[0]; p.jx = res_h[1]; p.jy = res_h[2]; p.jabs = res_h[3]; }
+        if (to_host) { p.rho = res_hd[0]; p.jx = res_hd[1]; p.jy = res_hd[2]; p.jabs = res_hd[3]; }
         p.lat0 = two_lattice() ? lat[par] : lat[0];
         p.lat1 = two_lattice() ? lat[par ^ 1u] : nullptr;
         p.jy_prev = jy_d + (size_t)par * H;
         p.jy_next = jy_d + (size_t)(par ^ 1u) * H;
         if (alg == 2) { p.halo_in = (double *)halo[par]; p.halo_out = (double *)halo[par ^ 1u]; }
+        if (debug) return plbm::launch_debug_step(prec, lay, alg == 1, p, block, stream);
         switch (alg) {
         case 0: return plbm::launch_nptl(prec, lay, p, grid, block, stream, porous);
         case 1: return plbm::launch_lptl(prec, lay, p, grid, block, stream, porous);
@@ -799,10 +902,13 @@ struct plbm_handler {
     // The Q60 form records a population that left its fixed-point range in a device word.
     void check_status()
     {
-        if (prec != PLBM_F64_Q60) return;
+        if (prec != PLBM_F64_Q60 && prec != PLBM_F16C) return;
         int st = 0;
         cuda_check(cudaMemcpyAsync(&st, status_d, sizeof(int), cudaMemcpyDeviceToHost, stream), "status");
         cuda_check(cudaStreamSynchronize(stream), "status");
+        if (st && prec == PLBM_F16C)
+            fail(PLBM_ERR_NUMERIC, "a population deviation left the f16c range (-0.5, 0.5) (unstable run?); rerun "
+                                   "with f32 or f16s");
         if (st)
             fail(PLBM_ERR_NUMERIC, "a population left the f64_q60 range [-4, 4) (unstable run?); rerun with f64_strict");
     }
@@ -848,6 +954,7 @@ struct plbm_handler {
     void loop()
     {
         try {
+            const PhaseTrace run_trace("run");
             cuda_check(cudaSetDevice(opt.device), "cudaSetDevice");
             const unsigned T = props.time_steps, F = props.frame_update_interval;
             unsigned t = iteration.load(), done = t, max_pending = 32;
@@ -868,7 +975,7 @@ struct plbm_handler {
                 unsigned frame = t + (F - 1 - t % F);
                 if (frame > T - 1) frame = T - 1;
                 unsigned end;
-                if (opt.use_graph && !export_fields && F >= 2 && F <= 256 && t % F == 0 && t + F < T) {
+                if (opt.use_graph && !export_fields && !debug && F >= 2 && F <= 256 && t % F == 0 && t + F < T) {
                     // a whole frame: one graph launch (its steps, results written to the host)
                     cuda_check(cudaGraphLaunch(frame_graph(t, F), stream), "frame graph launch");
                     end = t + F;
@@ -889,6 +996,7 @@ struct plbm_handler {
                 if (t - done >= max_pending) publish(t);
             }
             if (t != done) publish(t);
+            run_trace("steps and results done");
         } catch (const Status &s) {
             std::lock_guard<std::mutex> g(mu);
             worker_status = s.code;
@@ -974,7 +1082,7 @@ static int create_common(plbm_handler *h, const plbm_options *opt, plbm_handler 
         if (h->opt.mask) {
             Props p = h->from_json ? json_to_props(h->settings_path, 0, nullptr) : h->props;
             const size_t n = (size_t)(p.horizontal_nodes - 2) * (p.vertical_nodes - 2);
-            h->user_mask.assign(h->opt.mask, h->opt.mask + n);   // kept for initialize()
+            h->mask_n = n;
             h->has_mask = true;
             h->mask_src = h->opt.mask;                             // valid during this call only
             h->opt.mask = nullptr;
@@ -1312,8 +1420,7 @@ int plbm_sync_results(plbm_handler *h)
 
 int plbm_launches_per_step(plbm_handler *h, unsigned *n)
 {
-    (void)h;
-    *n = 1;
+    *n = h->debug ? 3 : 1;
     return PLBM_OK;
 }
 

@@ -179,17 +179,25 @@ template <int PREC> __device__ __forceinline__ float2 vec_unpack(unsigned w, flo
         __half2 h = *reinterpret_cast<__half2 *>(&w);
         const float2 v = __half22float2(h);
         return make_float2(v.x + shift, v.y + shift);
+    } else if constexpr (PREC == F16C) {
+        return make_float2(f16c_value(w & 0xffffu) + shift, f16c_value(w >> 16) + shift);
     } else {
         __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&w);
         const float2 v = __bfloat1622float2(h);
         return make_float2(v.x + shift, v.y + shift);
     }
 }
-template <int PREC> __device__ __forceinline__ unsigned vec_pack(float lo, float hi)
+// F16C: a value beyond the format's range sets `over` (the caller reports it once per thread).
+template <int PREC> __device__ __forceinline__ unsigned vec_pack(float lo, float hi, bool &over)
 {
     if constexpr (PREC == F16S) {
         __half2 h = __floats2half2_rn(lo, hi);
         return *reinterpret_cast<unsigned *>(&h);
+    } else if constexpr (PREC == F16C) {
+        bool o1, o2;
+        const unsigned a = f16c_bits(lo, o1), b = f16c_bits(hi, o2);
+        over |= o1 | o2;
+        return a | (b << 16);
     } else {
         __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
         return *reinterpret_cast<unsigned *>(&h);
@@ -226,7 +234,7 @@ __device__ __forceinline__ void vec_node(float f[9], int x, int y, uint16_t lk, 
 template <int PREC>
 __device__ __forceinline__ void vec_row_segment(const StepParams &p, int y, int xv, int lane)
 {
-    static_assert(PREC == F16S || PREC == BF16S, "2-byte shifted storage only");
+    static_assert(PREC == F16S || PREC == BF16S || PREC == F16C, "2-byte shifted storage only");
     const bool vec_ok = xv < p.P;
     const int x0 = vec_ok ? xv : p.P - VEC;                    // clamped: every lane loads inside the row
     const unsigned short *S = static_cast<const unsigned short *>(p.lat0);
@@ -266,6 +274,7 @@ __device__ __forceinline__ void vec_row_segment(const StepParams &p, int y, int 
         for (int d = 0; d < 9; ++d) r[d][0] = r[d][1] = r[d][2] = r[d][3] = 0u;
     }
     const unsigned lw[4] = { l4.x, l4.y, l4.z, l4.w };
+    bool over = false;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {     // one pair of nodes at a time
         float fa[9], fb[9];
@@ -282,8 +291,10 @@ __device__ __forceinline__ void vec_row_segment(const StepParams &p, int y, int 
         vec_node<PREC>(fa, xa, y, la, inner_row, vec_ok && xa < p.W && (la & LINK_FLUID), p);
         vec_node<PREC>(fb, xb, y, lb, inner_row, vec_ok && xb < p.W && (lb & LINK_FLUID), p);
 #pragma unroll
-        for (int d = 0; d < 9; ++d) r[d][k] = vec_pack<PREC>(fa[d], fb[d]);
+        for (int d = 0; d < 9; ++d) r[d][k] = vec_pack<PREC>(fa[d], fb[d], over);
     }
+    if constexpr (PREC == F16C)
+        if (over) atomicOr(p.status, 1);
     if (!vec_ok) return;
     unsigned short *D = static_cast<unsigned short *>(p.lat1);
 #pragma unroll
@@ -325,18 +336,20 @@ __global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::b
 
 // ---- npol: in place, one tile per thread block --------------------------------------------
 
-// Halo snapshot layout (storage type T): columns first, then rows.
-//   col[b][y'][0..2] = dirs 2,5,8 of node (x' = (b+1)*TW - 1, y')   right edge of tile column b
-//   col[b][y'][3..5] = dirs 0,3,6 of node (x' = (b+1)*TW,     y')   left edge of tile column b+1
-//   row[b][x'][0..2] = dirs 6,7,8 of node (x', y' = (b+1)*TH - 1)   top edge of tile row b
-//   row[b][x'][3..5] = dirs 0,1,2 of node (x', y' = (b+1)*TH)       bottom edge of tile row b+1
+// Halo snapshot layout (storage type T), structure of arrays: columns first, then rows; one
+// contiguous line per (tile boundary b, slot k), so the lanes of a warp along a tile edge read and
+// write consecutive entries.
+//   col[b][0..2][y'] = dirs 2,5,8 of node (x' = (b+1)*TW - 1, y')   right edge of tile column b
+//   col[b][3..5][y'] = dirs 0,3,6 of node (x' = (b+1)*TW,     y')   left edge of tile column b+1
+//   row[b][0..2][x'] = dirs 6,7,8 of node (x', y' = (b+1)*TH - 1)   top edge of tile row b
+//   row[b][3..5][x'] = dirs 0,1,2 of node (x', y' = (b+1)*TH)       bottom edge of tile row b+1
 __device__ __forceinline__ unsigned long long halo_col(const StepParams &p, int b, int y, int k)
 {
-    return ((unsigned long long)b * p.H + y) * 6 + k;
+    return ((unsigned long long)b * 6 + k) * p.H + y;
 }
 __device__ __forceinline__ unsigned long long halo_row(const StepParams &p, int b, int x, int k)
 {
-    return (unsigned long long)p.n_col_bounds * p.H * 6 + ((unsigned long long)b * p.W + x) * 6 + k;
+    return (unsigned long long)p.n_col_bounds * p.H * 6 + ((unsigned long long)b * 6 + k) * p.W + x;
 }
 
 template <int PREC, int L>

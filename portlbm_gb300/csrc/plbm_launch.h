@@ -16,6 +16,9 @@ cudaError_t launch_lptl(int prec, int lay, const StepParams &p, dim3 grid, dim3 
 cudaError_t launch_count_obstacle_nodes(const uint16_t *links, int W, int H, int P, unsigned long long *counts,
                                         cudaStream_t s);
 cudaError_t launch_npol(int prec, int lay, const StepParams &p, dim3 grid, dim3 block, cudaStream_t s);
+// debugMode's unfused step of nptl (linear = false, 2-D blocks) or lptl (linear = true, the block's
+// thread count as a 1-D block): stream, observables, collide; F64_STRICT and F32_REF (k_debug.cu).
+cudaError_t launch_debug_step(int prec, int lay, bool linear, const StepParams &p, dim3 block, cudaStream_t s);
 cudaError_t launch_nsol(int prec, int lay, const StepParams &p, unsigned t, dim3 grid, dim3 block, cudaStream_t s);
 
 // Set-up kernels (plbm_util.cu).

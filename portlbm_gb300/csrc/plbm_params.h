@@ -6,7 +6,7 @@
 namespace plbm {
 
 enum Layout { COLLISION = 0, STREAM = 1, BUNDLE = 2 };
-enum Precision { F64_STRICT = 0, F64_FAST = 1, F32_REF = 2, F32 = 3, F16S = 4, BF16S = 5, F64_Q60 = 6 };
+enum Precision { F64_STRICT = 0, F64_FAST = 1, F32_REF = 2, F32 = 3, F16S = 4, BF16S = 5, F64_Q60 = 6, F16C = 7 };
 
 constexpr uint16_t LINK_FLUID = 1u << 4;
 // Set by k_links on the nodes of the first and last inner row and column: with it, an interior
@@ -18,6 +18,17 @@ constexpr uint16_t LINK_EDGE = 1u << 9;
 // maximum, 65504.  The FP16 form also computes on these scaled values (its constants are scaled
 // the same way), so loads and stores need no rescaling.
 constexpr float F16_SCALE = 4096.0f;
+
+// F16C storage: the deviation df in a 16-bit float of 1 sign, 4 exponent and 11 significand bits
+// (the layout of a float32 with its exponent limited to 0..15 and its significand cut to 11 bits),
+// scaled so that |df| < 0.5 is representable: normal values from 2^-16, gradual underflow below
+// with a resolution of 2^-27.  IEEE half spends 5 exponent bits on a range the deviations never
+// use; this form gives that bit to the significand (relative rounding 2^-12 instead of 2^-11).
+// Decoding places the 15 magnitude bits in a float32 pattern and multiplies by 2^110; encoding
+// multiplies by 2^-110 and rounds the pattern to 11 significand bits (nearest, ties to even).
+constexpr float F16C_DECODE = 1.2980742146337069e33f;   // 2^110
+constexpr float F16C_ENCODE = 7.7037197775489434e-34f;  // 2^-110
+constexpr unsigned F16C_MAX_BITS = 0x7FFFu;            // largest magnitude pattern: (2 - 2^-11) * 2^-2
 
 // Nodes per thread of the two-lattice kernels (nptl rows, lptl grid strides), per precision.
 constexpr int rows_per_thread(int) { return 1; }
@@ -54,7 +65,7 @@ struct StepParams {
     // the device word that records a population leaving the fixed-point range
     long long q_weight[9], q_feq_in[9], q_feq_out[9];
     long long q_om1, q_ow49, q_ow9, q_ow36, q_k9, q_k36, q_o9, q_o36, q_rho_out, q_sixth, q_two_thirds;
-    int *status;
+    int *status;                // F64_Q60 / F16C: set when a value leaves the storage range
     int outlet_mode;            // 0: Zou/He-type density outlet; 1: constant feq(outlet) ghost
     int nan_protection;
     int write_results;          // this step is copied to the host

@@ -97,6 +97,7 @@ __global__ void k_fill_lattice(void *lat, int lay, unsigned long long N, W9 w)
         if constexpr (PREC == F64_Q60) b[i] = double_to_q(w.w[d]);
         else if constexpr (PREC == F16S) b[i] = __float2half_rn(0.0f);
         else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(0.0f);
+        else if constexpr (PREC == F16C) b[i] = 0;
         else b[i] = (T)w.w[d];
     }
 }
@@ -111,6 +112,7 @@ cudaError_t launch_fill_lattice(void *lat, int prec, int lay, unsigned long long
     case F32_REF: case F32: k_fill_lattice<F32><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
     case F16S: k_fill_lattice<F16S><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
     case BF16S: k_fill_lattice<BF16S><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
+    case F16C: k_fill_lattice<F16C><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
     case F64_Q60: k_fill_lattice<F64_Q60><<<grid, block, 0, s>>>(lat, lay, N, ww); break;
     default: return cudaErrorInvalidValue;
     }
@@ -134,7 +136,10 @@ __global__ void k_fill_shifted(void *lat, int lay, int P, unsigned long long N, 
         const float v = (float)(w.w[d] * ((1.0 - a) + g * x));
         if constexpr (PREC == F16S) static_cast<__half *>(lat)[i] = __float2half_rn(v * F16_SCALE);
         else if constexpr (PREC == BF16S) static_cast<__nv_bfloat16 *>(lat)[i] = __float2bfloat16_rn(v);
-        else static_cast<float *>(lat)[i] = v;
+        else if constexpr (PREC == F16C) {
+            bool over;   // the host admits the form only where the rest state's deviations fit
+            static_cast<unsigned short *>(lat)[i] = (unsigned short)f16c_bits(v, over);
+        } else static_cast<float *>(lat)[i] = v;
     }
 }
 
@@ -148,6 +153,7 @@ cudaError_t launch_fill_shifted(void *lat, int prec, int lay, int P, unsigned lo
     case F32: k_fill_shifted<F32><<<grid, block, 0, s>>>(lat, lay, P, N, ww, a, g); break;
     case F16S: k_fill_shifted<F16S><<<grid, block, 0, s>>>(lat, lay, P, N, ww, a, g); break;
     case BF16S: k_fill_shifted<BF16S><<<grid, block, 0, s>>>(lat, lay, P, N, ww, a, g); break;
+    case F16C: k_fill_shifted<F16C><<<grid, block, 0, s>>>(lat, lay, P, N, ww, a, g); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -156,19 +162,25 @@ cudaError_t launch_fill_shifted(void *lat, int prec, int lay, int P, unsigned lo
 // Halo snapshot entries hold the rest state initially (w_d, or 0 for the shifted forms, whose
 // npol lattice stores f - w_d); the direction of each slot follows the layout documented at k_npol.
 template <int PREC>
-__global__ void k_fill_halo(void *halo, unsigned long long ncol, unsigned long long total, W9 w)
+__global__ void k_fill_halo(void *halo, unsigned long long ncol, unsigned long long total, int W, int H, W9 w)
 {
     using T = typename Store<PREC>::T;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
          i += (unsigned long long)gridDim.x * blockDim.x) {
-        const int k = (int)(i % 6);
-        int d;
-        if (i < ncol) d = k < 3 ? 3 * k + 2 : 3 * (k - 3);
-        else d = k < 3 ? 6 + k : k - 3;
+        // slot k of the [b][k][line] layout (halo_col / halo_row in plbm_kernels.cuh)
+        int k, d;
+        if (i < ncol) {
+            k = (int)((i / (unsigned long long)H) % 6);
+            d = k < 3 ? 3 * k + 2 : 3 * (k - 3);
+        } else {
+            k = (int)(((i - ncol) / (unsigned long long)W) % 6);
+            d = k < 3 ? 6 + k : k - 3;
+        }
         T *b = static_cast<T *>(halo);
         if constexpr (PREC == F64_Q60) b[i] = double_to_q(w.w[d]);
         else if constexpr (PREC == F16S) b[i] = __float2half_rn(0.0f);
         else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(0.0f);
+        else if constexpr (PREC == F16C) b[i] = 0;
         else if constexpr (PREC == F32) b[i] = 0.0f;
         else b[i] = (T)w.w[d];
     }
@@ -182,12 +194,13 @@ cudaError_t launch_fill_halo(void *halo, int prec, int W, int H, int ncb, int nr
     if (total == 0) return cudaSuccess;
     const int grid = 152 * 2, block = 256;
     switch (prec) {
-    case F64_STRICT: case F64_FAST: k_fill_halo<F64_STRICT><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
-    case F32_REF: k_fill_halo<F32_REF><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
-    case F32: k_fill_halo<F32><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
-    case F16S: k_fill_halo<F16S><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
-    case BF16S: k_fill_halo<BF16S><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
-    case F64_Q60: k_fill_halo<F64_Q60><<<grid, block, 0, s>>>(halo, ncol, total, ww); break;
+    case F64_STRICT: case F64_FAST: k_fill_halo<F64_STRICT><<<grid, block, 0, s>>>(halo, ncol, total, W, H, ww); break;
+    case F32_REF: k_fill_halo<F32_REF><<<grid, block, 0, s>>>(halo, ncol, total, W, H, ww); break;
+    case F32: k_fill_halo<F32><<<grid, block, 0, s>>>(halo, ncol, total, W, H, ww); break;
+    case F16S: k_fill_halo<F16S><<<grid, block, 0, s>>>(halo, ncol, total, W, H, ww); break;
+    case BF16S: k_fill_halo<BF16S><<<grid, block, 0, s>>>(halo, ncol, total, W, H, ww); break;
+    case F16C: k_fill_halo<F16C><<<grid, block, 0, s>>>(halo, ncol, total, W, H, ww); break;
+    case F64_Q60: k_fill_halo<F64_Q60><<<grid, block, 0, s>>>(halo, ncol, total, W, H, ww); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -323,7 +336,7 @@ cudaError_t launch_set_equilibrium(void *lat, int prec, int lay, const StepParam
         else k_set_equilibrium<PR, BUNDLE><<<grid, block, 0, s>>>(lat, p, rho, jx, jy);                   \
         break;
     switch (prec) {
-        PLBM_EQ(F64_STRICT) PLBM_EQ(F64_FAST) PLBM_EQ(F32_REF) PLBM_EQ(F32) PLBM_EQ(F16S) PLBM_EQ(BF16S) PLBM_EQ(F64_Q60)
+        PLBM_EQ(F64_STRICT) PLBM_EQ(F64_FAST) PLBM_EQ(F32_REF) PLBM_EQ(F32) PLBM_EQ(F16S) PLBM_EQ(BF16S) PLBM_EQ(F64_Q60) PLBM_EQ(F16C)
     default: return cudaErrorInvalidValue;
     }
 #undef PLBM_EQ

@@ -1,7 +1,7 @@
 """Generates tests/golden/*.npz from the reference's own code (oracle/_ref, built from the
-reference tree by oracle/build_ref.py).  Run in the development container:
+reference tree by oracle/build_ref.py).  Run in the development container, naming the tree:
 
-    python tests/golden/make_golden.py
+    PORTLBM_REFERENCE=<reference tree> python tests/golden/make_golden.py
 
 Each case records the reference's rho, jx, jy, |j| after N steps (float64; the USE_FLOAT build's
 values converted exactly) and its core::Domain.  cases.json lists the parameters.  The cases cover

@@ -61,7 +61,7 @@ def test_q60_within_tolerance(plbm, oracle_mod, alg, lay):
     assert maxdiff(got, ref) <= 1e-12
 
 
-@pytest.mark.parametrize("precision", ["f16s", "bf16s"])
+@pytest.mark.parametrize("precision", ["f16s", "bf16s", "f16c"])
 @pytest.mark.parametrize("w,h,porous", [(203, 61, True), (300, 40, True), (62, 30, False), (520, 20, True)])
 def test_vectorised_rows_match_scalar_kernel(plbm, precision, w, h, porous):
     """nptl/stream runs the 2-byte forms 8 nodes per thread with warp shuffles (open gather); lptl,
@@ -79,7 +79,7 @@ def test_vectorised_rows_match_scalar_kernel(plbm, precision, w, h, porous):
             assert np.array_equal(a[k], b[k]), k
 
 
-@pytest.mark.parametrize("precision", ["f32", "f16s", "f64_strict"])
+@pytest.mark.parametrize("precision", ["f32", "f16s", "f16c", "f64_strict"])
 @pytest.mark.parametrize("alg,lay", [("nptl", "stream"), ("nptl", "bundle"), ("lptl", "collision")])
 def test_gather_forms_agree(plbm, precision, alg, lay):
     """The open and the porous gather give bit-identical results on a porous channel; "auto"
@@ -101,11 +101,11 @@ def test_gather_forms_agree(plbm, precision, alg, lay):
 
 
 # relative L2 of the momentum field / max |rho| difference against f64_strict after 600 steps
-SHIFTED_TOL = {"f32": (1e-4, 2e-6), "f16s": (2e-3, 2e-4), "bf16s": (2e-2, 2e-3)}
+SHIFTED_TOL = {"f32": (1e-4, 2e-6), "f16s": (2e-3, 2e-4), "bf16s": (2e-2, 2e-3), "f16c": (1e-3, 1e-4)}
 
 
 @pytest.mark.parametrize("alg", ALGS)
-@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s"])
+@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s", "f16c"])
 @pytest.mark.parametrize("lay,porous", [("stream", False), ("stream", True), ("collision", True), ("bundle", False)])
 def test_shifted_forms_track_fp64(plbm, alg, precision, lay, porous):
     """Every algorithm and data layout in the FP32/FP16/BF16 storage forms stays within its storage
@@ -304,7 +304,7 @@ def _batch_domains(plbm, n=5, seed=11, wmax=140):
     return doms
 
 
-@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s", "f64_q60"])
+@pytest.mark.parametrize("precision", ["f32", "f16s", "bf16s", "f16c", "f64_q60"])
 @pytest.mark.parametrize("mode", ["persistent", "persistent_graph", "per_domain"])
 @pytest.mark.parametrize("wide", [False, True])
 @pytest.mark.parametrize("vec_rows", [False, True])
@@ -332,7 +332,7 @@ def test_batch_equals_independent_handlers(plbm, precision, mode, wide, vec_rows
     b.close()
 
 
-@pytest.mark.parametrize("precision", ["f32", "f16s"])
+@pytest.mark.parametrize("precision", ["f32", "f16s", "f16c"])
 def test_batch_autotune_keeps_results(plbm, precision):
     """Autotuning times real steps (7 tile shapes x 3 occupancies x 2 steps, twice that for 2-byte
     storage, which also tries vectorised rows) and results do not depend on the tile it picks."""
@@ -340,7 +340,7 @@ def test_batch_autotune_keeps_results(plbm, precision):
     a = plbm.Batch(doms, precision=precision)
     a.autotune(steps=2)
     a.run(58)
-    tuned = 2 * 21 * (2 if precision == "f16s" else 1)
+    tuned = 2 * 21 * (2 if precision in ("f16s", "f16c") else 1)
     ref = plbm.Batch(doms, precision=precision)
     ref.run(tuned + 58, mode="per_domain")
     for i in range(len(doms)):
@@ -348,3 +348,11 @@ def test_batch_autotune_keeps_results(plbm, precision):
             assert np.array_equal(a.result(i, k), ref.result(i, k))
     na, _ = a.info()
     assert na == sum(d["mask"].size for d in doms)
+
+
+def test_f16c_rejects_boundaries_beyond_its_range(plbm):
+    """f16c stores deviations |f - w rho0| < 0.5: an inlet density of 3.5 puts the rest
+    population's deviation beyond that and creation fails with a numeric error."""
+    props = plbm.Properties("nptl", "stream", False, 64, 10, 10, "circle", 30, 62, 0.0, 0.0, 3.5, 0.0, 0.0, 1.0, 0.6)
+    with pytest.raises(plbm.Exception, match="f16c"):
+        plbm.create_handler(props, precision="f16c")
