@@ -67,15 +67,16 @@ def peaks() -> dict:
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons every 100 ms while running; summary() keeps the
-    samples whose nvidia-smi timestamp falls inside the timed steps' wall-clock window."""
+    """Samples nvidia-smi clocks and throttle reasons every `interval_ms` while running; summary()
+    keeps the samples whose nvidia-smi timestamp falls inside the timed steps' wall-clock window."""
 
     FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index: int = 0):
+    def __init__(self, index: int = 0, interval_ms: int = 20):
         self.index = index
+        self.interval_ms = interval_ms
         self.proc = None
         self.lines: list[str] = []
         self._t = None
@@ -84,7 +85,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.interval_ms)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
         except Exception:
@@ -229,10 +230,17 @@ def parity_drift(plbm, w=2000, h=500, checkpoints=(1000, 2000, 5000, 10000), tau
         for c in checkpoints:
             o.run(c - done)
             ref = [o.result(i) for i in range(3)]
-            row = {"tau": tau, "steps": c}
-            for p, hd in hds.items():
-                hd.run_steps(c - done)
-                hd.sync_results()
+            row = {"tau": tau, "steps": c,
+                   "oracle_max_abs_j": float(max(np.nanmax(np.abs(ref[1])), np.nanmax(np.abs(ref[2]))))}
+            for p, hd in list(hds.items()):
+                try:
+                    hd.run_steps(c - done)
+                    hd.sync_results()
+                except plbm.Exception as e:   # an unstable run leaves the form's range: recorded, not fatal
+                    row[p] = f"stopped: {e}"
+                    hd.close()
+                    del hds[p]
+                    continue
                 got = [hd.get_densities(), hd.get_x_velocities(), hd.get_y_velocities()]
                 row[p] = max(float(np.max(np.abs(a - b))) for a, b in zip(got, ref))
             done = c
@@ -248,16 +256,17 @@ TRAFFIC_PER_NODE = {"nptl_stream_f64_q60": 2.293e9 / (4096 * 4096), "nptl_stream
                     "nptl_stream_f32": 1.1375e9 / (4096 * 4096), "nptl_stream_f16s": 0.5923e9 / (4096 * 4096)}
 
 
-def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, max_steps=200000,
+def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, max_steps=100000,
                     ref_target=1e-9, ref_cap=400000, big=(8192, 8192), big_steps=2000, big_cap=None, small=True,
                     forms=("f64_strict", "f64_fast", "f32", "f16s", "f16c", "bf16s")):
     """Each storage form against the FP64 steady state on a seeded porous channel (disks r in [3, 12],
     tau 0.6, rho 1.01 / 1.0).  The reference steady state is f64_q60 (FP64 accuracy, <= 1e-12 from
-    the drop-in) run to residual `ref_target`; every form runs to residual `target` (at most
-    `max_steps` steps) and reports its steps, final residual, relative L2 error of the momentum
-    field and relative total-mass difference against that reference.  (A reference stopped at the
-    forms' own target would still be ~1e-3 away from its steady state and would charge its own
-    transient to the forms.)  Then the same errors on the 8192^2 porous channel against f64_q60,
+    the drop-in) run to residual `ref_target`; every form reports its steps and time to residual
+    `target` (None where rounding keeps it above), then runs on towards `ref_target` (at most
+    `max_steps` steps in all) and reports its final residual and the relative L2 error of its
+    momentum field and relative total-mass difference against that reference.  (A run stopped at
+    residual 1e-6 is still ~2e-3 from its steady state, so comparing there would charge the
+    transient to the form.)  Then the same errors on the 8192^2 porous channel against f64_q60,
     after `big_steps` steps or, with `big_cap`, run to `target` with at most `big_cap` steps."""
     mask = plbm.porous_disks(w, h, seed, porosity)
     fluid = mask.reshape(-1) == 0
@@ -278,6 +287,22 @@ def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, 
         hd.close()
         return n, r, dt, out
 
+    def run_to_steady(prec, mk, ww, hh):
+        """Steps and time to residual `target`, then on to `ref_target` (the form's steady state, or
+        its rounding plateau) within `max_steps` in all; the fields are those of the end."""
+        props = plbm.Properties("nptl", "stream", False, 1024, 10 ** 9, 10 ** 9, "Hagen-Poiseuille", hh, ww, 0.0,
+                                0.0, 1.01, 0.0, 0.0, 1.0, 0.6)
+        hd = plbm.create_handler(props, precision=prec, mask=mk)
+        t0 = time.perf_counter()
+        n1, r1 = hd.run_to_residual(target, 100, max_steps)
+        dt = time.perf_counter() - t0
+        n2, r2 = hd.run_to_residual(ref_target, 100, max_steps - n1) if n1 < max_steps else (0, r1)
+        out = (hd.get_densities(), hd.get_x_velocities(), hd.get_y_velocities())
+        hd.close()
+        reached = r1 < target
+        return {"steps_to_target": n1 if reached else None, "seconds_to_target": round(dt, 3) if reached else None,
+                "steps": n1 + n2, "residual": r2}, out
+
     def errs(a, b, fl):
         ja = np.concatenate([a[1][fl], a[2][fl]])
         jb = np.concatenate([b[1][fl], b[2][fl]])
@@ -291,10 +316,9 @@ def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, 
                       "reference": {"precision": "f64_q60", "steps": nref, "residual": rref,
                                     "seconds": round(tref, 3)}})
         for prec in forms:
-            n, r, dt, out = run(prec, mask, w, h)
+            rec, out = run_to_steady(prec, mask, w, h)
             l2, dm = errs(out, ref, fluid)
-            study[prec] = {"steps": n, "residual": r, "seconds": round(dt, 3), "rel_l2_j_vs_f64": l2,
-                           "mass_rel_diff_vs_f64": dm}
+            study[prec] = dict(rec, rel_l2_j_vs_f64=l2, mass_rel_diff_vs_f64=dm)
     bw, bh = big
     bmask = plbm.porous_disks(bw, bh, seed, porosity)
     bfl = bmask.reshape(-1) == 0
@@ -461,6 +485,18 @@ def barrier(world: int):
         dist.barrier()
 
 
+METRIC = "MLUPS (FP64 D2Q9 BGK, 8192x8192 circle channel)"
+
+
+def line_config(args, world) -> dict:
+    """The `config` of both arms' JSON lines (the reference arm reports the same workload)."""
+    w, h = args.width, args.height
+    return {"workload": f"circle channel {w}x{h} (r=H/8 at W/4), {args.algorithm}+{args.layout}, tau 0.6, "
+                        f"rho 1.2/1.0", "algorithm": args.algorithm, "data_layout": args.layout,
+            "precision": args.precision, "l2": "inputs larger than L2 (lattice %.1f GB)" % (2 * 9 * 8 * w * h / 1e9),
+            "parallelism": f"replicas{world}"}
+
+
 def run_reference(args, world, rank, budget_s=90.0):
     """Reference arm: the CPU oracle on the host cores, rank 0 only.  Each step is a bounded sample
     of the workload: when the whole run would take more than `budget_s`, the steps are taken over
@@ -478,7 +514,7 @@ def run_reference(args, world, rank, budget_s=90.0):
         m = mask if rows == h else mask[(h - rows) // 2:(h - rows) // 2 + rows].copy()
         m[0, :] = 1
         m[-1, :] = 1
-        return plbm_oracle.Oracle("nptl", "stream", 1024, "Hagen-Poiseuille", w, rows, inlet_density=1.2,
+        return plbm_oracle.Oracle(args.algorithm, args.layout, 1024, "Hagen-Poiseuille", w, rows, inlet_density=1.2,
                                   relaxation_time=0.6, mask=np.ascontiguousarray(m))
 
     rows = h
@@ -501,12 +537,11 @@ def run_reference(args, world, rank, budget_s=90.0):
     mlups = w * rows * args.steps / dt / 1e6
     sample = (f"{args.steps} full {w}x{h} timesteps" if rows == h else
               f"{args.steps} timesteps of a {w}x{rows} band of the {w}x{h} channel (full width, the disk)")
-    line = {"metric": "MLUPS (FP64 D2Q9 BGK, 8192x8192 circle channel)", "value": round(mlups, 2), "unit": "MLUPS",
+    line = {"metric": METRIC, "value": round(mlups, 2), "unit": "MLUPS",
             "impl": "reference", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1e3 * dt / args.steps, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"circle channel {w}x{h}, nptl+stream, tau 0.6, rho 1.2/1.0", "algorithm": "nptl",
-                       "data_layout": "stream", "precision": "f64"},
+            "config": line_config(args, world),
             "cpu_baseline": {"value": round(mlups, 2), "unit": "MLUPS", "cores": plbm_oracle.threads(),
                              "kind": "port",
                              "sample": f"{sample} of the CPU oracle (restated reference, OpenMP) after warm-up"},
@@ -585,9 +620,12 @@ def main():
     # -- device-resident timed region (value + roofline) --
     barrier(world)
     window = []
-    with ClockSampler(local) as clocks:
-        ms, hd = device_run(plbm, args.precision, args.algorithm, args.layout, w, h, mask, args.steps, args.warmup,
-                            window=window)
+    # sampled from the first device step to the end of the e2e and variant runs: `clocks` keeps the
+    # timed window, `clocks_run` every sample of that busy stretch
+    clocks = ClockSampler(local).__enter__()
+    run_t0 = time.time()
+    ms, hd = device_run(plbm, args.precision, args.algorithm, args.layout, w, h, mask, args.steps, args.warmup,
+                        window=window)
     barrier(world)
     ms = max_over_ranks(ms, world)
     launches = hd.launches_per_step() * args.steps
@@ -598,6 +636,7 @@ def main():
     hd.close()
 
     if args.kernel_only:
+        clocks.__exit__()
         if rank == 0:
             print(json.dumps({"value": round(value, 1), "unit": "MLUPS", "ms_per_step": round(ms, 4),
                               "achieved_gbs": round(achieved_gbs, 1), "precision": args.precision}), flush=True)
@@ -624,6 +663,8 @@ def main():
         variants["ratios"] = {f"{p}_over_{q}": round(variants[p]["mlups"] / variants[q]["mlups"], 3)
                               for p in ("f16s", "f16c") for q in ("f64_q60", "f64_strict")}
 
+    run_t1 = time.time()
+    clocks.__exit__()
     err = None
     if rank == 0:
         err = {"poiseuille_400x100_2000_steps": err_vs_oracle(plbm, args.precision),
@@ -645,15 +686,12 @@ def main():
     if rank == 0:
         traffic = load_traffic(f"{args.algorithm}_{args.layout}_{args.precision}", w * h)
         line = {
-            "metric": "MLUPS (FP64 D2Q9 BGK, 8192x8192 circle channel)",
+            "metric": METRIC,
             "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int64 (Q3.60 fixed point, FP64 accuracy)" if args.precision == "f64_q60" else "f64",
             "data": "synthetic", "err_vs_oracle": err,
-            "config": {"workload": f"circle channel {w}x{h} (r=H/8 at W/4), nptl+stream, tau 0.6, rho 1.2/1.0",
-                       "algorithm": args.algorithm, "data_layout": args.layout, "precision": args.precision,
-                       "l2": "inputs larger than L2 (lattice %.1f GB)" % (2 * 9 * 8 * w * h / 1e9),
-                       "parallelism": f"replicas{world}"},
+            "config": line_config(args, world),
             "roofline": {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                          "frac": round(achieved_gbs / pk["hbm_gbs"], 4), "traffic": traffic,
                          # DRAM bytes the launch actually moves (ncu traffic; solid nodes move none)
@@ -667,6 +705,7 @@ def main():
                     "d2h_bytes_per_step": round(4 * 8 * w * h / e2e_steps)},
             "gpu_launches": launches,
             "clocks": clocks.summary(window),
+            "clocks_run": clocks.summary((run_t0, run_t1)),
             "cpu_baseline": cpu,
             "variants": variants,
             "precision_study": study,

@@ -34,7 +34,8 @@ def test_reference_arm_samples_a_band_when_the_run_would_be_long(capsys):
     exceed its time budget it steps a centred band of the channel and says so in `sample`."""
     import argparse
     import json
-    args = argparse.Namespace(width=256, height=160, steps=3, warmup=1)
+    args = argparse.Namespace(width=256, height=160, steps=3, warmup=1, algorithm="nptl", layout="stream",
+                              precision="f64_q60")
     bench.run_reference(args, 1, 0, budget_s=1e-6)
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["steps"] == 3 and line["value"] > 0
@@ -43,3 +44,5 @@ def test_reference_arm_samples_a_band_when_the_run_would_be_long(capsys):
     bench.run_reference(args, 1, 0, budget_s=1e6)
     line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
     assert line["cpu_baseline"]["sample"].startswith("3 full 256x160 timesteps")
+    # the reference arm reports the same config as the measured arm
+    assert line["config"] == bench.line_config(args, 1) and line["metric"] == bench.METRIC
