@@ -85,7 +85,9 @@ GATHER = {"auto": 0, "open": 1, "porous": 2}
 
 
 def library_path() -> str:
-    return os.path.join(_HERE, "libplbm.so")
+    """libplbm.so, or the bounds-checked build libplbm_checked.so when PLBM_CHECKED=1."""
+    name = "libplbm_checked.so" if os.environ.get("PLBM_CHECKED") == "1" else "libplbm.so"
+    return os.path.join(_HERE, name)
 
 
 _LIB = None

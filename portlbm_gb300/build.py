@@ -4,6 +4,11 @@ Every translation unit is compiled in parallel with nvcc for ``-gencode
 arch=compute_103a,code=sm_103a`` only, then linked into ``portlbm_gb300/libplbm.so``
 with the CUDA runtime linked statically (the library has no run-time dependency on a
 particular libcudart path).  Run ``python -m portlbm_gb300.build``.
+
+``build(checked=True)`` (``python -m portlbm_gb300.build --checked``) compiles the same sources
+with -DPLBM_CHECKED into ``libplbm_checked.so``: every index of the step kernels is compared with
+its buffer's extent and an out-of-range access is skipped and reported as an error.  The package
+loads it instead of libplbm.so when PLBM_CHECKED=1 is set in the environment.
 """
 from __future__ import annotations
 
@@ -17,6 +22,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libplbm.so")
+LIB_CHECKED = os.path.join(PKG, "libplbm_checked.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["k_nptl.cu", "k_lptl.cu", "k_npol.cu", "k_nsol.cu", "k_debug.cu", "plbm_util.cu", "plbm_noalloc.cu", "plbm_batch.cu", "plbm_nn.cu", "plbm_nn_tc.cu"]
 CPP_SOURCES = ["plbm_host.cpp", "plbm_benchmark.cpp"]
@@ -37,25 +43,29 @@ def _sources_mtime() -> float:
     return max(newest, os.path.getmtime(__file__))
 
 
-def up_to_date() -> bool:
-    return os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime()
+def up_to_date(checked: bool = False) -> bool:
+    lib = LIB_CHECKED if checked else LIB
+    return os.path.exists(lib) and os.path.getmtime(lib) >= _sources_mtime()
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and up_to_date():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> str:
+    lib = LIB_CHECKED if checked else LIB
+    if not force and up_to_date(checked):
+        return lib
+    build_dir = BUILD + ("_checked" if checked else "")
+    os.makedirs(build_dir, exist_ok=True)
     cc = nvcc()
-    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo", "-I", CSRC,
+    defs = ["-DPLBM_CHECKED"] if checked else []
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo", *defs, "-I", CSRC,
               "-I", os.path.join(os.path.dirname(PKG), "include")]
     jobs = []
     for src in CU_SOURCES:
-        obj = os.path.join(BUILD, src + ".o")
+        obj = os.path.join(build_dir, src + ".o")
         jobs.append([cc, *ARCH, *common, "-c", os.path.join(CSRC, src), "-o", obj])
     cuda_inc = os.path.join(os.path.dirname(os.path.dirname(cc)), "include")
     for src in CPP_SOURCES:
-        obj = os.path.join(BUILD, src + ".o")
-        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unknown-pragmas", "-I", cuda_inc,
+        obj = os.path.join(build_dir, src + ".o")
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unknown-pragmas", *defs, "-I", cuda_inc,
                      "-I", CSRC, "-c", os.path.join(CSRC, src), "-o", obj])
 
     def run(cmd):
@@ -68,14 +78,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(run, jobs))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     link = [cc, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-lpthread"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + " ".join(link) + "\n" + r.stdout + r.stderr)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose=True))
+    print(build(force="--force" in sys.argv, verbose=True, checked="--checked" in sys.argv))

@@ -42,12 +42,12 @@ __global__ void k_debug_stream(StepParams p)
     int xi, yi;
     unsigned long long n;
     if (!debug_node<LINEAR>(p, xi, yi, n)) return;
-    const uint16_t lk = p.links[n];
+    const uint16_t lk = link_at(p, n);
     if (!(lk & LINK_FLUID)) return;
     CT<PREC> f[9];
 #pragma unroll
     for (int d = 0; d < 9; ++d) f[d] = pull_one<PREC, L>(p.lat0, n, xi, yi, d, lk, p);
-    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
+    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, jy_prev_at(p, yi), p);
 #pragma unroll
     for (int d = 0; d < 9; ++d) st<PREC>(p.lat1, lidx<L>(n, d, p.N), d, f[d], p);
 }
@@ -83,7 +83,7 @@ __global__ void k_debug_observables(StepParams p)
     int xi, yi;
     unsigned long long n;
     if (!debug_node<LINEAR>(p, xi, yi, n)) return;
-    if (!(p.links[n] & LINK_FLUID)) return;
+    if (!(link_at(p, n) & LINK_FLUID)) return;
     using R = CT<PREC>;
     R f[9];
 #pragma unroll
@@ -98,9 +98,10 @@ __global__ void k_debug_observables(StepParams p)
         if (p.nan_protection) { rho = nan_guard_f(rho); jx = nan_guard_f(jx); jy = nan_guard_f(jy); ja = nan_guard_f(ja); }
     }
     const unsigned long long r = (unsigned long long)xi + (unsigned long long)yi * p.W;
+    if (!in_range(r, (unsigned long long)p.W * p.H, p)) return;
     p.rho[r] = rho; p.jx[r] = jx; p.jy[r] = jy; p.jabs[r] = ja;
     // the outlet reads this step's jy of column W-2 (the reference reads the result array)
-    if (xi == p.W - 2 && p.jy_next) p.jy_next[yi] = jy;
+    if (xi == p.W - 2 && p.jy_next && in_range((unsigned long long)yi, (unsigned long long)p.H, p)) p.jy_next[yi] = jy;
 }
 
 template <int PREC, int L, bool LINEAR>
@@ -109,8 +110,12 @@ __global__ void k_debug_collide(StepParams p)
     int xi, yi;
     unsigned long long n;
     if (!debug_node<LINEAR>(p, xi, yi, n)) return;
-    if (!(p.links[n] & LINK_FLUID)) return;
+    if (!(link_at(p, n) & LINK_FLUID)) return;
     const unsigned long long r = (unsigned long long)xi + (unsigned long long)yi * p.W;
+    // lidx(n, 0) and lidx(n, 8) bound the node's nine entries in every layout
+    if (!in_range(r, (unsigned long long)p.W * p.H, p) || !in_range(lidx<L>(n, 8, p.N), p.lat_elems, p) ||
+        !in_range(lidx<L>(n, 0, p.N), p.lat_elems, p))
+        return;
     if constexpr (PREC == F64_STRICT) {
         const double rho = p.rho[r], ux = p.jx[r], uy = p.jy[r];
         const double usq = __dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy));

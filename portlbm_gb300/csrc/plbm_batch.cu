@@ -356,6 +356,7 @@ int plbm_batch_create(unsigned n, const plbm_batch_domain *doms, int precision, 
         double *jyc = (double *)ptrs[5];
         d.nan_protection = 1;
         d.status = b->status_pending;
+        d.lat_elems = 9ull * d.N;
         e = cudaMemcpyAsync(flags, s.mask, (size_t)d.W * d.H, cudaMemcpyHostToDevice, b->stream);
         if (e == cudaSuccess) e = plbm::launch_links(flags, (uint16_t *)ptrs[2], d.W, d.H, d.P, b->stream);
         double rest[9];
@@ -447,6 +448,8 @@ int plbm_batch_run(plbm_batch *b, unsigned steps, int mode, double *ms_per_step)
     if (ms_per_step) *ms_per_step = steps ? ms / steps : 0.0;
     int st = 0;
     cudaMemcpy(&st, b->status_d, sizeof(int), cudaMemcpyDeviceToHost);
+    if (st & plbm::STATUS_OUT_OF_RANGE)
+        return berr(b, PLBM_ERR_CUDA, "checked build: a batch kernel computed an index outside its buffer");
     if (st)
         return berr(b, PLBM_ERR_NUMERIC, b->prec == PLBM_F16C ? "a population deviation left the f16c range"
                                                               : "a population left the f64_q60 range");

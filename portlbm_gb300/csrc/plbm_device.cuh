@@ -37,6 +37,39 @@ __device__ __forceinline__ unsigned long long lidx(unsigned long long n, int d, 
     return 3ull * (d / 3) * N + (d % 3) + 3ull * n;
 }
 
+// Index test of the checked build (see STATUS_OUT_OF_RANGE): true when i < n; otherwise records
+// the out-of-range index in the status word and returns false so the caller skips the access.
+// Without PLBM_CHECKED it is the constant true and costs nothing.
+__device__ __forceinline__ bool in_range(unsigned long long i, unsigned long long n, const StepParams &p)
+{
+#ifdef PLBM_CHECKED
+    if (i < n) return true;
+    if (p.status) atomicOr(p.status, STATUS_OUT_OF_RANGE);
+    return false;
+#else
+    (void)i; (void)n; (void)p;
+    return true;
+#endif
+}
+
+// Entries of the buffer a population load or store addresses: a lattice or the npol halo.
+__device__ __forceinline__ unsigned long long pop_extent(const void *base, const StepParams &p)
+{
+    return (base == p.halo_in || base == p.halo_out) ? p.halo_elems : p.lat_elems;
+}
+
+// links[n], n < N
+__device__ __forceinline__ uint16_t link_at(const StepParams &p, unsigned long long n)
+{
+    return in_range(n, p.N, p) ? p.links[n] : (uint16_t)0;
+}
+
+// jy of column W-2 in the previous step, y' < H
+__device__ __forceinline__ double jy_prev_at(const StepParams &p, int y)
+{
+    return in_range((unsigned long long)y, (unsigned long long)p.H, p) ? p.jy_prev[y] : 0.0;
+}
+
 // D2Q9 direction d: cx = d % 3 - 1, cy = d / 3 - 1 (access.hpp:203-213).
 __device__ __forceinline__ int cxd(int d) { return d % 3 - 1; }
 __device__ __forceinline__ int cyd(int d) { return d / 3 - 1; }
@@ -85,7 +118,8 @@ __device__ __forceinline__ typename Store<PREC>::C ld(const void *base, unsigned
 {
     using T = typename Store<PREC>::T;
     const T *b = static_cast<const T *>(base);
-    (void)d; (void)p;
+    (void)d;
+    if (!in_range(i, pop_extent(base, p), p)) return typename Store<PREC>::C(0);
     if constexpr (PREC == F16S) return __half2float(b[i]);   // df * F16_SCALE, the FP16 form's compute value
     else if constexpr (PREC == BF16S) return __bfloat162float(b[i]);
     else if constexpr (PREC == F16C) return f16c_value(b[i]);
@@ -97,7 +131,8 @@ __device__ __forceinline__ void st(void *base, unsigned long long i, int d, type
 {
     using T = typename Store<PREC>::T;
     T *b = static_cast<T *>(base);
-    (void)d; (void)p;
+    (void)d;
+    if (!in_range(i, pop_extent(base, p), p)) return;
     if constexpr (PREC == F16S) b[i] = __float2half_rn(v);
     else if constexpr (PREC == BF16S) b[i] = __float2bfloat16_rn(v);
     else if constexpr (PREC == F16C) {
@@ -462,11 +497,13 @@ template <int PREC> __device__ __forceinline__ typename Store<PREC>::C g_out(con
 __device__ __forceinline__ void write_observables(const Moments &m, int xi, int yi, const StepParams &p)
 {
     double rho = m.rho, jx = m.jx, jy = m.jy;
-    if (xi == p.W - 2 && p.jy_next) p.jy_next[yi] = p.nan_protection ? nan_guard(jy) : jy;
+    if (xi == p.W - 2 && p.jy_next && in_range((unsigned long long)yi, (unsigned long long)p.H, p))
+        p.jy_next[yi] = p.nan_protection ? nan_guard(jy) : jy;
     if (p.write_results) {
         double ja = sqrt(m.usq);
         if (p.nan_protection) { rho = nan_guard(rho); jx = nan_guard(jx); jy = nan_guard(jy); ja = nan_guard(ja); }
         const unsigned long long r = (unsigned long long)xi + (unsigned long long)yi * p.W;
+        if (!in_range(r, (unsigned long long)p.W * p.H, p)) return;
         p.rho[r] = rho; p.jx[r] = jx; p.jy[r] = jy; p.jabs[r] = ja;
     }
 }
@@ -475,11 +512,13 @@ __device__ __forceinline__ void write_observables(const Moments &m, int xi, int 
 __device__ __forceinline__ void write_observables_f32ref(const Moments &m, int xi, int yi, const StepParams &p)
 {
     double rho = m.rho, jx = m.jx, jy = m.jy;
-    if (xi == p.W - 2 && p.jy_next) p.jy_next[yi] = p.nan_protection ? nan_guard(jy) : jy;
+    if (xi == p.W - 2 && p.jy_next && in_range((unsigned long long)yi, (unsigned long long)p.H, p))
+        p.jy_next[yi] = p.nan_protection ? nan_guard(jy) : jy;
     if (p.write_results) {
         double ja = (double)sqrtf((float)m.usq);
         if (p.nan_protection) { rho = nan_guard(rho); jx = nan_guard(jx); jy = nan_guard(jy); ja = nan_guard(ja); }
         const unsigned long long r = (unsigned long long)xi + (unsigned long long)yi * p.W;
+        if (!in_range(r, (unsigned long long)p.W * p.H, p)) return;
         p.rho[r] = rho; p.jx[r] = jx; p.jy[r] = jy; p.jabs[r] = ja;
     }
 }

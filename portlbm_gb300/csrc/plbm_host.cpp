@@ -763,6 +763,7 @@ struct plbm_handler {
         b.links = links;
         b.rho = res_d[0]; b.jx = res_d[1]; b.jy = res_d[2]; b.jabs = res_d[3];
         b.W = W; b.H = H; b.P = P; b.N = N;
+        b.lat_elems = 9ull * N;
         b.outlet_mode = outlet_mode;
         b.nan_protection = opt.nan_protection;
 
@@ -798,6 +799,7 @@ struct plbm_handler {
             b.n_col_bounds = (int)grid.x - 1;
             b.n_row_bounds = (int)grid.y - 1;
             const size_t hn = (size_t)b.n_col_bounds * H * 6 + (size_t)b.n_row_bounds * W * 6;
+            b.halo_elems = hn;
             for (auto &hp : halo) {
                 cuda_check(cudaMalloc(&hp, std::max<size_t>(hn, 1) * eb), "cudaMalloc halo");
                 cuda_check(plbm::launch_fill_halo(hp, prec, W, H, b.n_col_bounds, b.n_row_bounds, rest, stream),
@@ -902,10 +904,13 @@ struct plbm_handler {
     // The Q60 form records a population that left its fixed-point range in a device word.
     void check_status()
     {
-        if (prec != PLBM_F64_Q60 && prec != PLBM_F16C) return;
+        if (prec != PLBM_F64_Q60 && prec != PLBM_F16C && !plbm::CHECKED_BUILD) return;
         int st = 0;
         cuda_check(cudaMemcpyAsync(&st, status_d, sizeof(int), cudaMemcpyDeviceToHost, stream), "status");
         cuda_check(cudaStreamSynchronize(stream), "status");
+        if (st & plbm::STATUS_OUT_OF_RANGE)
+            fail(PLBM_ERR_CUDA, "checked build: a step kernel computed an index outside its buffer (the access was "
+                                "skipped)");
         if (st && prec == PLBM_F16C)
             fail(PLBM_ERR_NUMERIC, "a population deviation left the f16c range (-0.5, 0.5) (unstable run?); rerun "
                                    "with f32 or f16s");
@@ -1449,6 +1454,9 @@ const char *plbm_last_error(const plbm_handler *h)
     return g_tls_error.c_str();
 }
 
-const char *plbm_version(void) { return "portlbm_gb300 0.1 (sm_103a)"; }
+const char *plbm_version(void)
+{
+    return plbm::CHECKED_BUILD ? "portlbm_gb300 0.2 (sm_103a, checked)" : "portlbm_gb300 0.2 (sm_103a)";
+}
 
 }  // extern "C"

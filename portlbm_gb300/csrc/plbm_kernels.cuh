@@ -96,7 +96,7 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
     for (int j = 0; j < NY; ++j) {
         const bool in = xi[j] < p.W && yi[j] < p.H;
         n[j] = in ? (unsigned long long)xi[j] + (unsigned long long)yi[j] * p.P : 0;
-        lk[j] = in ? p.links[n[j]] : 0;
+        lk[j] = in ? link_at(p, n[j]) : 0;
     }
 #pragma unroll
     for (int j = 0; j < NY; ++j) {
@@ -131,7 +131,7 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
                     if (cxd(d) != 0 && !((lk[j] >> d) & 1u)) f[j][d] += p.shift_cx[d];
             }
         }
-        if (is_outlet_row(xi[j], yi[j], p)) outlet_fill<PREC>(f[j], p.jy_prev[yi[j]], p);
+        if (is_outlet_row(xi[j], yi[j], p)) outlet_fill<PREC>(f[j], jy_prev_at(p, yi[j]), p);
         const auto m = collide<PREC>(f[j], p);
 #pragma unroll
         for (int d = 0; d < 9; ++d) st<PREC>(p.lat1, lidx<L>(n[j], d, p.N), d, f[j][d], p);
@@ -211,7 +211,7 @@ __device__ __forceinline__ void vec_edge_gather(float *f, int x, int y, uint16_t
     const unsigned long long n = (unsigned long long)x + (unsigned long long)y * p.P;
 #pragma unroll
     for (int d = 0; d < 9; ++d) f[d] = pull_one<PREC, STREAM>(p.lat0, n, x, y, d, lk, p);
-    if (is_outlet_row(x, y, p)) outlet_fill<PREC>(f, p.jy_prev[y], p);
+    if (is_outlet_row(x, y, p)) outlet_fill<PREC>(f, jy_prev_at(p, y), p);
 }
 
 template <int PREC>
@@ -243,11 +243,14 @@ __device__ __forceinline__ void vec_row_segment(const StepParams &p, int y, int 
 
     // r[d][k]: plane d's values for nodes x0 + 2k (low half) and x0 + 2k + 1 (high half)
     unsigned r[9][4];
-    const uint4 l4 = *reinterpret_cast<const uint4 *>(p.links + row0 + x0);
+    const uint4 l4 = in_range(row0 + x0 + VEC - 1, p.N, p) ? *reinterpret_cast<const uint4 *>(p.links + row0 + x0)
+                                                         : make_uint4(0, 0, 0, 0);
     if (inner_row) {
 #pragma unroll
         for (int d = 0; d < 9; ++d) {   // all nine loads are issued before any is used
-            const uint4 v = *reinterpret_cast<const uint4 *>(S + (size_t)d * p.N + (size_t)(y - cyd(d)) * p.P + x0);
+            const size_t at = (size_t)d * p.N + (size_t)(y - cyd(d)) * p.P + x0;
+            const uint4 v = in_range(at + VEC - 1, p.lat_elems, p) ? *reinterpret_cast<const uint4 *>(S + at)
+                                                                  : make_uint4(0, 0, 0, 0);
             r[d][0] = v.x; r[d][1] = v.y; r[d][2] = v.z; r[d][3] = v.w;
         }
 #pragma unroll
@@ -255,14 +258,17 @@ __device__ __forceinline__ void vec_row_segment(const StepParams &p, int y, int 
             const unsigned short *row = S + (size_t)d * p.N + (size_t)(y - cyd(d)) * p.P;
             if (cxd(d) == 1) {            // source x - 1: shift up by one node, the previous lane's last node in front
                 unsigned prev = __shfl_up_sync(0xffffffffu, r[d][3] >> 16, 1);
-                if (lane == 0) prev = x0 >= 1 ? (unsigned)row[x0 - 1] : 0u;
+                if (lane == 0)
+                    prev = x0 >= 1 && in_range((size_t)(row - S) + x0 - 1, p.lat_elems, p) ? (unsigned)row[x0 - 1] : 0u;
                 r[d][3] = __byte_perm(r[d][2], r[d][3], 0x5432);
                 r[d][2] = __byte_perm(r[d][1], r[d][2], 0x5432);
                 r[d][1] = __byte_perm(r[d][0], r[d][1], 0x5432);
                 r[d][0] = __byte_perm(prev, r[d][0], 0x5410);
             } else if (cxd(d) == -1) {    // source x + 1: shift down by one node, the next lane's first node behind
                 unsigned next = __shfl_down_sync(0xffffffffu, r[d][0] & 0xffffu, 1);
-                if (lane == 31) next = x0 + VEC < p.P ? (unsigned)row[x0 + VEC] : 0u;
+                if (lane == 31)
+                    next = x0 + VEC < p.P && in_range((size_t)(row - S) + x0 + VEC, p.lat_elems, p) ? (unsigned)row[x0 + VEC]
+                                                                                                    : 0u;
                 r[d][0] = __byte_perm(r[d][0], r[d][1], 0x5432);
                 r[d][1] = __byte_perm(r[d][1], r[d][2], 0x5432);
                 r[d][2] = __byte_perm(r[d][2], r[d][3], 0x5432);
@@ -298,8 +304,11 @@ __device__ __forceinline__ void vec_row_segment(const StepParams &p, int y, int 
     if (!vec_ok) return;
     unsigned short *D = static_cast<unsigned short *>(p.lat1);
 #pragma unroll
-    for (int d = 0; d < 9; ++d)
-        *reinterpret_cast<uint4 *>(D + (size_t)d * p.N + row0 + x0) = make_uint4(r[d][0], r[d][1], r[d][2], r[d][3]);
+    for (int d = 0; d < 9; ++d) {
+        const size_t at = (size_t)d * p.N + row0 + x0;
+        if (in_range(at + VEC - 1, p.lat_elems, p))
+            *reinterpret_cast<uint4 *>(D + at) = make_uint4(r[d][0], r[d][1], r[d][2], r[d][3]);
+    }
 }
 
 template <int PREC>
@@ -360,7 +369,7 @@ __global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::b
     const int xi = tcx * TW + threadIdx.x, yi = tcy * TH + threadIdx.y;
     const bool inside = xi < p.W && yi < p.H;
     const unsigned long long n = inside ? (unsigned long long)xi + (unsigned long long)yi * p.P : 0;
-    const uint16_t lk = inside ? p.links[n] : 0;
+    const uint16_t lk = inside ? link_at(p, n) : 0;
     const bool fluid = (lk & LINK_FLUID) != 0;
     const int lx = threadIdx.x, ly = threadIdx.y;
     CT<PREC> f[9];
@@ -390,7 +399,7 @@ __global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::b
     }
     __syncthreads();   // every read of this tile's old values happens before any write
     if (!fluid) return;
-    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
+    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, jy_prev_at(p, yi), p);
     const auto m = collide<PREC>(f, p);
 #pragma unroll
     for (int d = 0; d < 9; ++d) st<PREC>(p.lat0, lidx<L>(n, d, p.N), d, f[d], p);
@@ -418,7 +427,7 @@ __global__ void k_nsol_even(StepParams p)
     const int yi = blockIdx.y * blockDim.y + threadIdx.y;
     if (xi >= p.W || yi >= p.H) return;
     const unsigned long long n = (unsigned long long)xi + (unsigned long long)yi * p.P;
-    const uint16_t lk = p.links[n];
+    const uint16_t lk = link_at(p, n);
     if (!(lk & LINK_FLUID)) return;
     CT<PREC> f[9];
     const bool fast = lk == LINK_FLUID;   // links carry LINK_EDGE on the domain edge
@@ -441,7 +450,7 @@ __global__ void k_nsol_even(StepParams p)
             }
         }
     }
-    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
+    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, jy_prev_at(p, yi), p);
     const auto m = collide<PREC>(f, p);
     if (fast) {
 #pragma unroll
@@ -465,7 +474,7 @@ __global__ void k_nsol_odd(StepParams p)
     const int yi = blockIdx.y * blockDim.y + threadIdx.y;
     if (xi >= p.W || yi >= p.H) return;
     const unsigned long long n = (unsigned long long)xi + (unsigned long long)yi * p.P;
-    const uint16_t lk = p.links[n];
+    const uint16_t lk = link_at(p, n);
     if (!(lk & LINK_FLUID)) return;
     CT<PREC> f[9];
     if (lk == LINK_FLUID) {   // links carry LINK_EDGE on the domain edge
@@ -487,7 +496,7 @@ __global__ void k_nsol_odd(StepParams p)
             }
         }
     }
-    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, p.jy_prev[yi], p);
+    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, jy_prev_at(p, yi), p);
     const auto m = collide<PREC>(f, p);
 #pragma unroll
     for (int d = 0; d < 9; ++d) st<PREC>(p.lat0, lidx<L>(n, 8 - d, p.N), 8 - d, f[d], p);

@@ -52,7 +52,7 @@ __global__ void k_nptl_noalloc(plbm::StepParams p, const int8_t *flags)
     double f[9];
 #pragma unroll
     for (int d = 0; d < 9; ++d) f[d] = pull_one<F64_STRICT, STREAM>(p.lat0, n, xi, yi, d, lk, p);
-    if (is_outlet_row(xi, yi, p)) outlet_fill<F64_STRICT>(f, p.jy_prev[yi], p);
+    if (is_outlet_row(xi, yi, p)) outlet_fill<F64_STRICT>(f, jy_prev_at(p, yi), p);
     const Moments m = collide<F64_STRICT>(f, p);
 #pragma unroll
     for (int d = 0; d < 9; ++d) st<F64_STRICT>(p.lat1, lidx<STREAM>(n, d, p.N), d, f[d], p);
@@ -133,6 +133,7 @@ extern "C" int plbm_nptl_steps_noalloc(const plbm_noalloc_args *a)
     p.omega = 1 / a->relaxation_time;
     p.rho_out = a->outlet_density;
     p.W = W; p.H = H; p.P = P; p.N = N;
+    p.lat_elems = 9ull * N;
     p.nan_protection = a->nan_protection;
     double *res = static_cast<double *>(a->results);
     p.rho = res; p.jx = res + nres; p.jy = res + 2 * nres; p.jabs = res + 3 * nres;

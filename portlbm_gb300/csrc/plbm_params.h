@@ -30,6 +30,17 @@ constexpr float F16C_DECODE = 1.2980742146337069e33f;   // 2^110
 constexpr float F16C_ENCODE = 7.7037197775489434e-34f;  // 2^-110
 constexpr unsigned F16C_MAX_BITS = 0x7FFFu;            // largest magnitude pattern: (2 - 2^-11) * 2^-2
 
+// The checked build (compiled with -DPLBM_CHECKED, libplbm_checked.so) compares every lattice,
+// link, result, jy-column and halo index of the step kernels with its buffer's extent; an index
+// outside it sets this bit of the status word and the access is skipped (no trap).  The host turns
+// the bit into PLBM_ERR_CUDA after the steps.
+constexpr int STATUS_OUT_OF_RANGE = 0x100;
+#ifdef PLBM_CHECKED
+constexpr bool CHECKED_BUILD = true;
+#else
+constexpr bool CHECKED_BUILD = false;
+#endif
+
 // Nodes per thread of the two-lattice kernels (nptl rows, lptl grid strides), per precision.
 constexpr int rows_per_thread(int) { return 1; }
 
@@ -65,7 +76,10 @@ struct StepParams {
     // the device word that records a population leaving the fixed-point range
     long long q_weight[9], q_feq_in[9], q_feq_out[9];
     long long q_om1, q_ow49, q_ow9, q_ow36, q_k9, q_k36, q_o9, q_o36, q_rho_out, q_sixth, q_two_thirds;
-    int *status;                // F64_Q60 / F16C: set when a value leaves the storage range
+    int *status;                // F64_Q60 / F16C: bit 0 when a value leaves the storage range;
+                                // checked builds: STATUS_OUT_OF_RANGE when an index leaves its buffer
+    // Buffer extents (entries) for the checked build's index tests: each lattice, the npol halo.
+    unsigned long long lat_elems, halo_elems;
     int outlet_mode;            // 0: Zou/He-type density outlet; 1: constant feq(outlet) ghost
     int nan_protection;
     int write_results;          // this step is copied to the host

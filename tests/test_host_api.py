@@ -211,3 +211,18 @@ def test_porous_disks_generator(plbm):
     assert abs((1 - m[1:-1].mean()) - 0.7) < 0.01
     assert np.array_equal(m, plbm.porous_disks(300, 120, 5, 0.7))      # seeded
     assert not np.array_equal(m, plbm.porous_disks(300, 120, 6, 0.7))
+
+
+def test_checked_build_loads_and_exports_the_same_symbols(plbm):
+    """libplbm_checked.so (PLBM_CHECKED) builds from the same sources, exports every entry point of
+    libplbm.so and says which build it is; loading it needs no GPU."""
+    import ctypes
+    import subprocess
+    from portlbm_gb300 import build as b
+    lib = ctypes.CDLL(b.build(checked=True))
+    lib.plbm_version.restype = ctypes.c_char_p
+    assert b"checked" in lib.plbm_version()
+    out = subprocess.run(["nm", "-D", "--defined-only", b.LIB_CHECKED], capture_output=True, text=True).stdout
+    ref = subprocess.run(["nm", "-D", "--defined-only", b.LIB], capture_output=True, text=True).stdout
+    names = lambda t: {ln.split()[-1] for ln in t.splitlines() if " T plbm_" in ln}  # noqa: E731
+    assert names(ref) and names(ref) == names(out)
