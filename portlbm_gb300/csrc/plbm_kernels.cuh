@@ -71,6 +71,62 @@ __device__ __forceinline__ void emit_observables(const MomentsOf<PREC> &m, int x
     }
 }
 
+// Launch bounds of the nptl, lptl and npol step kernels: the Q60 form runs 256-thread blocks and
+// is limited by memory latency, so it is held to 48 registers for a fifth resident block per SM
+// (measured faster despite a few spilled words; nsol measured equal and keeps its registers).
+template <int PREC> struct NptlBounds { static constexpr int threads = 512, blocks = 1; };
+template <> struct NptlBounds<F64_Q60> { static constexpr int threads = 256, blocks = 5; };
+
+// Collision (AoS) layout: the 32 nodes of a warp that lies in one row (or one run of the linear
+// index) own 32 consecutive records, 288 consecutive entries of the destination lattice.  Written
+// one direction at a time, a warp's 8-byte stores sit 72 bytes apart and touch 32 sectors each; when
+// every lane holds a fluid node the warp instead stages its records in a shared-memory slice of its
+// own (one __syncwarp, no block barrier) and writes the 288 entries as nine contiguous 32-lane stores
+// (8 sectors each).  Warps with a solid or padding lane keep the direct stores, so nodes that are
+// not fluid are never written, as before.
+template <int PREC> __host__ __device__ constexpr int stage_warps() { return NptlBounds<PREC>::threads / 32; }
+
+template <int PREC>
+__device__ __forceinline__ typename Store<PREC>::T encode_value(typename Store<PREC>::C v, const StepParams &p)
+{
+    if constexpr (PREC == F16S) return __float2half_rn(v);
+    else if constexpr (PREC == BF16S) return __float2bfloat16_rn(v);
+    else if constexpr (PREC == F16C) {
+        bool over;
+        const unsigned short b = (unsigned short)f16c_bits(v, over);
+        if (over) atomicOr(p.status, 1);
+        return b;
+    } else return v;
+}
+
+template <int PREC>
+__device__ __forceinline__ void store_records_staged(const StepParams &p, unsigned long long n, const CT<PREC> f[9],
+                                                     bool fluid)
+{
+    using T = typename Store<PREC>::T;
+    __shared__ T stage[stage_warps<PREC>()][9 * 32];
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned warp = (threadIdx.y * blockDim.x + threadIdx.x) >> 5;
+    if (__ballot_sync(0xffffffffu, fluid) != 0xffffffffu) {
+        if (fluid) {
+#pragma unroll
+            for (int d = 0; d < 9; ++d) st<PREC>(p.lat1, 9ull * n + d, d, f[d], p);
+        }
+        return;
+    }
+    T *slice = stage[warp];
+#pragma unroll
+    for (int d = 0; d < 9; ++d) slice[lane * 9 + d] = encode_value<PREC>(f[d], p);
+    __syncwarp();
+    const unsigned long long first = 9ull * (n - lane);   // the record of the warp's first node
+    T *dst = static_cast<T *>(p.lat1) + first;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        if (in_range(first + 32u * k + lane, p.lat_elems, p)) dst[32u * k + lane] = slice[32u * k + lane];
+    }
+    __syncwarp();
+}
+
 // Rows per thread: a node of the 2-byte forms moves only 36 B, so each thread issues the loads of
 // several nodes before computing any of them to keep enough bytes in flight per SM.
 template <int PREC> struct RowsPerThread { static constexpr int value = rows_per_thread(PREC); };
@@ -85,9 +141,12 @@ template <int PREC> struct RowsPerThread { static constexpr int value = rows_per
 //    re-referencing shift added after the branches (domains full of obstacles);
 //  * shifted storage otherwise: plain loads and the shift for interior nodes without solid
 //    neighbours, pull_one for the rest (open channels).
-template <int PREC, int L, int NY, bool POROUS = false>
+// STAGED (collision layout, NY == 1, called by whole warps whose 32 nodes are consecutive):
+// the destination records are written through store_records_staged.
+template <int PREC, int L, int NY, bool POROUS = false, bool STAGED = false>
 __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const int yi[NY], const StepParams &p)
 {
+    static_assert(!STAGED || (L == COLLISION && NY == 1), "staged stores: collision layout, one node per thread");
     constexpr bool SH = shifted<PREC>();
     CT<PREC> f[NY][9];
     uint16_t lk[NY];
@@ -120,32 +179,45 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
             for (int d = 0; d < 9; ++d) f[j][d] = pull_one<PREC, L>(p.lat0, n[j], xi[j], yi[j], d, lk[j], p);
         }
     }
+    if constexpr (STAGED) {
+        const bool fluid = (lk[0] & LINK_FLUID) != 0;
+        MomentsOf<PREC> m{};
+        if (fluid) {
+            if constexpr (SH && POROUS) {
+                if (!(lk[0] & LINK_EDGE)) {
 #pragma unroll
-    for (int j = 0; j < NY; ++j) {
-        if (!(lk[j] & LINK_FLUID)) continue;
-        if constexpr (SH && POROUS) {
-            // values pulled from the neighbouring columns are re-referenced to this node's rho0
-            if (!(lk[j] & LINK_EDGE)) {
-#pragma unroll
-                for (int d = 0; d < 9; ++d)
-                    if (cxd(d) != 0 && !((lk[j] >> d) & 1u)) f[j][d] += p.shift_cx[d];
+                    for (int d = 0; d < 9; ++d)
+                        if (cxd(d) != 0 && !((lk[0] >> d) & 1u)) f[0][d] += p.shift_cx[d];
+                }
             }
+            if (is_outlet_row(xi[0], yi[0], p)) outlet_fill<PREC>(f[0], jy_prev_at(p, yi[0]), p);
+            m = collide<PREC>(f[0], p);
         }
-        if (is_outlet_row(xi[j], yi[j], p)) outlet_fill<PREC>(f[j], jy_prev_at(p, yi[j]), p);
-        const auto m = collide<PREC>(f[j], p);
+        store_records_staged<PREC>(p, n[0], f[0], fluid);
+        if (fluid) emit_observables<PREC>(m, xi[0], yi[0], p);
+    } else {
 #pragma unroll
-        for (int d = 0; d < 9; ++d) st<PREC>(p.lat1, lidx<L>(n[j], d, p.N), d, f[j][d], p);
-        emit_observables<PREC>(m, xi[j], yi[j], p);
+        for (int j = 0; j < NY; ++j) {
+            if (!(lk[j] & LINK_FLUID)) continue;
+            if constexpr (SH && POROUS) {
+                // values pulled from the neighbouring columns are re-referenced to this node's rho0
+                if (!(lk[j] & LINK_EDGE)) {
+#pragma unroll
+                    for (int d = 0; d < 9; ++d)
+                        if (cxd(d) != 0 && !((lk[j] >> d) & 1u)) f[j][d] += p.shift_cx[d];
+                }
+            }
+            if (is_outlet_row(xi[j], yi[j], p)) outlet_fill<PREC>(f[j], jy_prev_at(p, yi[j]), p);
+            const auto m = collide<PREC>(f[j], p);
+#pragma unroll
+            for (int d = 0; d < 9; ++d) st<PREC>(p.lat1, lidx<L>(n[j], d, p.N), d, f[j][d], p);
+            emit_observables<PREC>(m, xi[j], yi[j], p);
+        }
     }
 }
 
 // nptl: 2-D blocks (tile shape from the work-group size hint); each thread updates NY
 // consecutive rows of its column.
-// Launch bounds of the nptl, lptl and npol step kernels: the Q60 form runs 256-thread blocks and
-// is limited by memory latency, so it is held to 48 registers for a fifth resident block per SM
-// (measured faster despite a few spilled words; nsol measured equal and keeps its registers).
-template <int PREC> struct NptlBounds { static constexpr int threads = 512, blocks = 1; };
-template <> struct NptlBounds<F64_Q60> { static constexpr int threads = 256, blocks = 5; };
 
 template <int PREC, int L, bool POROUS = false>
 __global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::blocks) k_nptl(StepParams p)
@@ -153,6 +225,16 @@ __global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::b
     constexpr int NY = RowsPerThread<PREC>::value;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y0 = (blockIdx.y * blockDim.y + threadIdx.y) * NY;
+    if constexpr (L == COLLISION && NY == 1) {
+        if ((blockDim.x & 31u) == 0) {
+            // whole warps lie in one row: leave (warp-uniformly) only past the last row or the
+            // padded row; lanes past W take part in the staged store as non-fluid nodes
+            if (y0 >= p.H || x - (int)(threadIdx.x & 31u) >= p.P) return;
+            const int xs[1] = { x }, ys[1] = { y0 };
+            update_two_lattice_rows<PREC, L, 1, POROUS, true>(xs, ys, p);
+            return;
+        }
+    }
     if (x >= p.W || y0 >= p.H) return;
     int xi[NY], yi[NY];
 #pragma unroll
@@ -339,6 +421,11 @@ __global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::b
             yi[j] = p.H;
             xi[j] = p.W;
         }
+    }
+    if constexpr (L == COLLISION && NY == 1) {
+        // blockDim.x is a multiple of 32: every warp covers 32 consecutive linear indices
+        update_two_lattice_rows<PREC, L, 1, POROUS, true>(xi, yi, p);
+        return;
     }
     update_two_lattice_rows<PREC, L, NY, POROUS>(xi, yi, p);
 }
