@@ -318,7 +318,8 @@ int plbm_nn_adam(float *w, const float *g, float *m, float *v, void *w_bf16, lon
 /* 1 when plbm_nn_conv_fwd runs the shape (input channels Cin, output channels Cout) on the
  * tcgen05 tensor-core kernel: Cin a multiple of 32, Cout <= 128, W a multiple of 128 or a power of
  * two below 128 with H a multiple of 128 / W.  plbm_nn_conv_dgrad uses it with the two channel
- * counts exchanged; other shapes and the weight gradient run the mma.sync kernel. */
+ * counts exchanged; plbm_nn_conv_wgrad runs on tcgen05 when, in addition, Cin <= 128 and Cout is a
+ * multiple of 32; other shapes run the mma.sync kernel. */
 int plbm_nn_conv_on_tensor_cores(int H, int W, int Cin, int Cout);
 /* Synchronises the device and reports whether a tensor-core convolution gave up on a wait (its
  * output is then invalid); clears the flag. */

@@ -17,6 +17,8 @@ bool plbm_nn_tc_supported(int H, int W, int Cin, int Cout);
 int plbm_nn_tc_conv(const void *x, const void *w, const float *bias, void *y, int N, int H, int W, int Cin, int Cout,
                     int relu, cudaStream_t s);
 int plbm_nn_tc_flip(const void *w, void *wt, int Cin, int Cout, cudaStream_t s);
+bool plbm_nn_tc_wgrad_supported(int H, int W, int Cin, int Cout);
+int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int W, int Cin, int Cout, cudaStream_t s);
 
 namespace {
 
@@ -352,11 +354,16 @@ int plbm_nn_conv_dgrad(const void *g, const void *w, void *gx, int N, int H, int
 int plbm_nn_conv_wgrad(const void *x, const void *g, float *gw, float *gb, int N, int H, int W, int Cin, int Cout,
                        void *stream)
 {
-    ConvArgs a{};
-    a.x = (const __nv_bfloat16 *)x; a.g = (const __nv_bfloat16 *)g; a.gw = gw;
-    a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout;
-    a.M = Cout; a.Ncols = 9 * Cin; a.K = N * H * W;
-    int rc = run_conv<WGRAD>(a, (cudaStream_t)stream);
+    int rc;
+    if (plbm_nn_tc_wgrad_supported(H, W, Cin, Cout)) {
+        rc = plbm_nn_tc_wgrad(x, g, gw, N, H, W, Cin, Cout, (cudaStream_t)stream);
+    } else {
+        ConvArgs a{};
+        a.x = (const __nv_bfloat16 *)x; a.g = (const __nv_bfloat16 *)g; a.gw = gw;
+        a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout;
+        a.M = Cout; a.Ncols = 9 * Cin; a.K = N * H * W;
+        rc = run_conv<WGRAD>(a, (cudaStream_t)stream);
+    }
     if (rc == PLBM_OK && gb) {
         const long long P = (long long)N * H * W;
         const long long gx = (P + 7) / 8 < 1024 ? (P + 7) / 8 : 1024;

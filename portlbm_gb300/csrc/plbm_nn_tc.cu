@@ -226,6 +226,163 @@ k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUte
     }
 }
 
+// ---- weight gradient ------------------------------------------------------------------------
+// dW[co][tap][ci] += sum over pixels p of g[p][co] * x[p + offset(tap)][ci]: a GEMM with M = Cout,
+// N = Cin per tap and K = the pixels.  Both operands arrive as TMA tiles of 128 pixels x 32
+// channels (64-byte rows, 64-byte swizzle), exactly the tiles of the forward kernel: a row is one
+// pixel, i.e. one K index, holding 32 consecutive M (or N) elements, so both are fed to tcgen05.mma
+// MN-major ("transposed" in the instruction descriptor).  In that layout a swizzle atom is 8 K-rows
+// of 32 MN elements; the stride byte offset steps 8 K-rows (512 B) and the leading byte offset
+// steps 32 MN elements (the next 32-channel tile, WG_CHUNK bytes on).  M is Cout padded to 128
+// (TMA fills the channels past Cout with zeros); each of the CTA's taps accumulates N = Cin TMEM
+// columns.  A CTA walks (pixel tile, tap) pairs of its share of the pixels (split K, one CTA per
+// SM) and adds its partial sums to dW with FP32 atomics.
+constexpr int WG_M = 128;                          // TMEM lanes: Cout padded
+constexpr int WG_CHUNK = TC_BM * TC_KB * 2;        // one 128-pixel x 32-channel tile, 8 KB
+constexpr int WG_A_BYTES = (WG_M / TC_KB) * WG_CHUNK;   // 32 KB
+constexpr int WG_SLACK = 16384;                    // keeps any reading of the descriptors inside the allocation
+
+struct WgArgs {
+    float *gw;
+    int N, H, W, Cin, Cout;
+    int BW, BH, tiles_x, tiles_y;
+    int ntaps;              // taps per CTA (3 or 9); blockIdx.y selects the group
+    int tiles_per_cta, total_tiles;
+    int b_bytes, stage_bytes, stages;
+    int *err;
+};
+
+// MN-major operand in 64-byte-swizzled rows: leading byte offset = next 32-element MN tile,
+// stride byte offset = next group of 8 K-rows (512 B).
+__device__ __forceinline__ uint64_t smem_desc_mn_sw64(unsigned addr, unsigned lbo_bytes)
+{
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo_bytes >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)(512 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)4 << 61);
+}
+
+// kind::f16, FP32 accumulator, BF16 A and B, both MN-major, M = 128, N = n.
+__device__ __forceinline__ unsigned instr_desc_mn(int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) | ((unsigned)(n >> 3) << 17) |
+           ((unsigned)(WG_M >> 4) << 24);
+}
+
+__global__ void __launch_bounds__(128, 1)
+k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap gmap, WgArgs a)
+{
+    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+    unsigned char *smem = tc_smem_raw + ((1024 - (smem_u32(tc_smem_raw) & 1023)) & 1023);
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + a.stages * a.stage_bytes + WG_SLACK);
+    unsigned long long *full = bars, *empty = bars + a.stages, *done = bars + 2 * a.stages;
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(bars + 2 * a.stages + 1);
+    int *counts = reinterpret_cast<int *>(tmem_slot + 1);   // [0] issued, [1] consumed, [2] failed
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cols = a.ntaps * a.Cin;
+    const unsigned ncols = cols <= 32 ? 32u : cols <= 64 ? 64u : cols <= 128 ? 128u : cols <= 256 ? 256u : 512u;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < a.stages; ++s) { mbar_init(smem_u32(&full[s]), 1); mbar_init(smem_u32(&empty[s]), 1); }
+        mbar_init(smem_u32(done), 1);
+        counts[0] = counts[1] = counts[2] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(ncols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = *tmem_slot;
+
+    const int tap0 = blockIdx.y * a.ntaps;
+    const int first = blockIdx.x * a.tiles_per_cta;
+    const int ntiles = max(0, min(a.tiles_per_cta, a.total_tiles - first));
+    const int iters = ntiles * a.ntaps;
+    const int per_img = a.tiles_x * a.tiles_y;
+    const int kbx = a.Cin / TC_KB;
+
+    if (warp == 0 && lane == 0) {              // producer: TMA loads of the g tile and the shifted x tile
+        for (int it = 0; it < iters; ++it) {
+            const int s = it % a.stages;
+            if (it >= a.stages && !mbar_wait(smem_u32(&empty[s]), (unsigned)((it / a.stages - 1) & 1))) {
+                counts[2] = 1;
+                break;
+            }
+            const int tile = first + it / a.ntaps, tap = tap0 + it % a.ntaps;
+            const int n = tile / per_img, t2 = tile % per_img;
+            const int y0 = (t2 / a.tiles_x) * a.BH, x0 = (t2 % a.tiles_x) * a.BW;
+            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+            unsigned char *st = smem + s * a.stage_bytes;
+            const unsigned bar = smem_u32(&full[s]);
+            mbar_expect_tx(bar, (unsigned)WG_A_BYTES + (unsigned)a.b_bytes);
+            for (int c = 0; c < WG_M / TC_KB; ++c)
+                tma_load_4d(smem_u32(st + c * WG_CHUNK), &gmap, c * TC_KB, x0, y0, n, bar);
+            for (int c = 0; c < kbx; ++c)
+                tma_load_4d(smem_u32(st + WG_A_BYTES + c * WG_CHUNK), &xmap, c * TC_KB, x0 + dx, y0 + dy, n, bar);
+            counts[0] = it + 1;
+        }
+    } else if (warp == 1 && lane == 0) {       // MMA issuer
+        const unsigned idesc = instr_desc_mn(a.Cin);
+        int it = 0;
+        for (; it < iters; ++it) {
+            const int s = it % a.stages;
+            if (!mbar_wait(smem_u32(&full[s]), (unsigned)((it / a.stages) & 1))) {
+                counts[2] = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const unsigned abase = smem_u32(smem + s * a.stage_bytes), bbase = abase + WG_A_BYTES;
+            const unsigned dcol = tmem + (unsigned)((it % a.ntaps) * a.Cin);
+            const bool first_tile = it < a.ntaps;
+#pragma unroll
+            for (int k = 0; k < TC_BM / 16; ++k)   // K = 16 pixels per MMA: two 8-row groups, 1 KB on
+                umma(dcol, smem_desc_mn_sw64(abase + 1024 * k, WG_CHUNK), smem_desc_mn_sw64(bbase + 1024 * k, WG_CHUNK),
+                     idesc, !(first_tile && k == 0));
+            umma_commit(smem_u32(&empty[s]));
+            counts[1] = it + 1;
+        }
+        umma_commit(smem_u32(done));
+    }
+    if (!mbar_wait(smem_u32(done), 0)) counts[2] = 1;
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool valid = *((volatile int *)&counts[2]) == 0;
+    const int co = warp * 32 + lane;
+    if (iters > 0) {
+        for (int c0 = 0; c0 < cols; c0 += 16) {
+            unsigned v[16];
+            const unsigned taddr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0;
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                           "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (!valid || co >= a.Cout) continue;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int col = c0 + j, t = col / a.Cin, ci = col % a.Cin;
+                atomicAdd(&a.gw[(size_t)co * 9 * a.Cin + (size_t)(tap0 + t) * a.Cin + ci], __uint_as_float(v[j]));
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && !valid) {
+        atomicExch(a.err, 1);
+        mbar_wait(smem_u32(done), 0);
+        for (int it = counts[1]; it < counts[0]; ++it)
+            mbar_wait(smem_u32(&full[it % a.stages]), (unsigned)((it / a.stages) & 1));
+    }
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+}
+
 // Wt[ci][tap][co] = W[co][8 - tap][ci]: the weights of the input-gradient convolution.
 __global__ void k_flip_weights(const __nv_bfloat16 *w, __nv_bfloat16 *wt, int Cin, int Cout)
 {
@@ -315,6 +472,59 @@ int plbm_nn_tc_conv(const void *x, const void *w, const float *bias, void *y, in
     TcArgs a{ (__nv_bfloat16 *)y, bias, N, H, W, Cin, Cout, npad, relu, BW, BH, W / BW, H / BH, stage, err };
     const int tiles = N * a.tiles_x * a.tiles_y;
     k_conv_tc<<<tiles, 128, TC_STAGES * stage + 1024 + 256, s>>>(xmap, wmap, a);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+// The weight gradient runs on the tensor cores for Cin and Cout multiples of 32 up to 128 and the
+// image tilings of the forward kernel.
+bool plbm_nn_tc_wgrad_supported(int H, int W, int Cin, int Cout)
+{
+    if (Cin % TC_KB != 0 || Cout % TC_KB != 0 || Cin > 128 || Cout > WG_M || Cin < TC_KB) return false;
+    return plbm_nn_tc_supported(H, W, Cin, Cout);
+}
+
+// gw[co][tap][ci] += sum_p g[p][co] x[p + tap][ci] on the tensor cores (x, g NHWC BF16, gw FP32).
+int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int W, int Cin, int Cout, cudaStream_t s)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    int *err = error_flag();
+    if (!enc || !err) return PLBM_ERR_CUDA;
+    const int BW = W >= TC_BM ? TC_BM : W, BH = TC_BM / BW;
+    const int ntaps = 9 * Cin <= 512 ? 9 : 3;
+    const int b_bytes = (Cin / TC_KB) * WG_CHUNK;
+    const int stage = WG_A_BYTES + b_bytes;
+    const int stages = (200 * 1024) / stage < 4 ? (200 * 1024) / stage : 4;
+    const int smem = stages * stage + WG_SLACK + 1024 + 256;
+    static int attr_bytes = 0;
+    static std::mutex mu;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (smem > attr_bytes) {
+            if (cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+                return PLBM_ERR_CUDA;
+            attr_bytes = smem;
+        }
+    }
+    CUtensorMap xmap, gmap;
+    const cuuint32_t es[4] = { 1, 1, 1, 1 };
+    for (int which = 0; which < 2; ++which) {
+        const int C = which == 0 ? Cin : Cout;
+        const cuuint64_t dims[4] = { (cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N };
+        const cuuint64_t strides[3] = { (cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2 };
+        const cuuint32_t box[4] = { TC_KB, (cuuint32_t)BW, (cuuint32_t)BH, 1 };
+        if (enc(which == 0 ? &xmap : &gmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(which == 0 ? x : g),
+                dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return PLBM_ERR_ARGUMENT;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    const int groups = 9 / ntaps;
+    const int total = N * (W / BW) * (H / BH);
+    const int chunks = (sms + groups - 1) / groups;
+    const int per = (total + chunks - 1) / chunks;
+    WgArgs a{ gw, N, H, W, Cin, Cout, BW, BH, W / BW, H / BH, ntaps, per, total, b_bytes, stage, stages, err };
+    k_wgrad_tc<<<dim3((total + per - 1) / per, groups), 128, smem, s>>>(xmap, gmap, a);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
 }
 

@@ -101,6 +101,31 @@ def test_tensor_core_convolution(plbm, n, h, w, cin, cout):
     assert lib.plbm_nn_status(ctypes.byref(failed)) == 0 and failed.value == 0
 
 
+@pytest.mark.parametrize("n,h,w,cin,cout", [(2, 8, 256, 32, 32), (1, 16, 128, 128, 96), (4, 16, 128, 64, 64),
+                                           (2, 32, 16, 32, 128), (1, 8, 64, 96, 32)])
+def test_tensor_core_weight_gradient(plbm, n, h, w, cin, cout):
+    """The weight gradient on tcgen05 (both operands MN-major TMA tiles, split over the pixels,
+    FP32 atomics) against the CPU oracle; it accumulates into gw like the other path."""
+    import torch
+    lib = _lib(plbm)
+    lib.plbm_nn_status.argtypes = [ctypes.POINTER(ctypes.c_int)]
+    rng = np.random.default_rng(11 * cin + cout)
+    x = nn_ref.bf16_round(rng.standard_normal((n, h, w, cin)))
+    g = nn_ref.bf16_round(rng.standard_normal((n, h, w, cout)))
+    rgw, rgb = nn_ref.conv_wgrad(x, g)
+    start = rng.standard_normal((cout, 9 * cin)).astype(np.float32)
+    gw = torch.tensor(start).cuda()
+    gb = torch.zeros(cout, dtype=torch.float32, device="cuda")
+    assert lib.plbm_nn_conv_wgrad(_bf(x).data_ptr(), _bf(g).data_ptr(), gw.data_ptr(), gb.data_ptr(), n, h, w, cin,
+                                  cout, None) == 0
+    torch.cuda.synchronize()
+    got = gw.cpu().numpy().astype(np.float64) - start
+    assert np.max(np.abs(got - rgw)) <= 1e-3 * np.max(np.abs(rgw)), np.max(np.abs(got - rgw))
+    assert np.max(np.abs(_np(gb) - rgb)) <= 1e-2 * np.max(np.abs(rgb)) + 1e-2
+    failed = ctypes.c_int(-1)
+    assert lib.plbm_nn_status(ctypes.byref(failed)) == 0 and failed.value == 0
+
+
 def test_pool_and_upsample(plbm):
     import torch
     lib = _lib(plbm)
