@@ -96,20 +96,21 @@ template <int PREC> __host__ __device__ constexpr bool shifted()
     return PREC == F32 || PREC == F16S || PREC == BF16S || PREC == F16C;
 }
 
-// The 16-bit F16C pattern <-> float (see F16C_DECODE in plbm_params.h).  f16c_bits returns the
-// pattern, saturated to the largest magnitude, and sets `over` when |v| >= 0.5 (or v is NaN).
+// The 16-bit F16C pattern <-> float (see F16C_DECODE in plbm_params.h).  f16c_bits rounds the
+// float32 pattern of v * 2^-110 to 11 significand bits (nearest, ties away from zero: ties are
+// one pattern in 2^12) and sets `over` when the magnitude does not fit, |v| >= 0.5 or v NaN (the
+// step then reports the status word and the run fails; the pattern itself is not meaningful).
 __device__ __forceinline__ float f16c_value(unsigned u)
 {
     return __uint_as_float(((u & 0x7FFFu) << 12) | ((u & 0x8000u) << 16)) * F16C_DECODE;
 }
+__device__ __forceinline__ unsigned f16c_round(unsigned b) { return ((b & 0x7FFFFFFFu) + 0x800u) >> 12; }
 __device__ __forceinline__ unsigned f16c_bits(float v, bool &over)
 {
     const unsigned b = __float_as_uint(v * F16C_ENCODE);
-    const unsigned mag = b & 0x7FFFFFFFu;
-    unsigned r = (mag + 0x7FFu + ((mag >> 12) & 1u)) >> 12;
-    over = r > F16C_MAX_BITS;
-    r = over ? F16C_MAX_BITS : r;
-    return r | ((b >> 16) & 0x8000u);
+    const unsigned r = f16c_round(b);
+    over = (r & ~F16C_MAX_BITS) != 0;
+    return (r & F16C_MAX_BITS) | ((b >> 16) & 0x8000u);
 }
 
 

@@ -99,9 +99,10 @@ __device__ __forceinline__ typename Store<PREC>::T encode_value(typename Store<P
     } else return v;
 }
 
-template <int PREC>
-__device__ __forceinline__ void store_records_staged(const StepParams &p, unsigned long long n, const CT<PREC> f[9],
-                                                     bool fluid)
+// dst: the lattice written; REVERSED writes value d into slot 8 - d (nsol's odd step).
+template <int PREC, bool REVERSED = false>
+__device__ __forceinline__ void store_records_staged(const StepParams &p, void *dst_lattice, unsigned long long n,
+                                                     const CT<PREC> f[9], bool fluid)
 {
     using T = typename Store<PREC>::T;
     __shared__ T stage[stage_warps<PREC>()][9 * 32];
@@ -110,16 +111,19 @@ __device__ __forceinline__ void store_records_staged(const StepParams &p, unsign
     if (__ballot_sync(0xffffffffu, fluid) != 0xffffffffu) {
         if (fluid) {
 #pragma unroll
-            for (int d = 0; d < 9; ++d) st<PREC>(p.lat1, 9ull * n + d, d, f[d], p);
+            for (int d = 0; d < 9; ++d) {
+                const int k = REVERSED ? 8 - d : d;
+                st<PREC>(dst_lattice, 9ull * n + k, k, f[d], p);
+            }
         }
         return;
     }
     T *slice = stage[warp];
 #pragma unroll
-    for (int d = 0; d < 9; ++d) slice[lane * 9 + d] = encode_value<PREC>(f[d], p);
+    for (int d = 0; d < 9; ++d) slice[lane * 9 + (REVERSED ? 8 - d : d)] = encode_value<PREC>(f[d], p);
     __syncwarp();
     const unsigned long long first = 9ull * (n - lane);   // the record of the warp's first node
-    T *dst = static_cast<T *>(p.lat1) + first;
+    T *dst = static_cast<T *>(dst_lattice) + first;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
         if (in_range(first + 32u * k + lane, p.lat_elems, p)) dst[32u * k + lane] = slice[32u * k + lane];
@@ -193,7 +197,7 @@ __device__ __forceinline__ void update_two_lattice_rows(const int xi[NY], const 
             if (is_outlet_row(xi[0], yi[0], p)) outlet_fill<PREC>(f[0], jy_prev_at(p, yi[0]), p);
             m = collide<PREC>(f[0], p);
         }
-        store_records_staged<PREC>(p, n[0], f[0], fluid);
+        store_records_staged<PREC>(p, p.lat1, n[0], f[0], fluid);
         if (fluid) emit_observables<PREC>(m, xi[0], yi[0], p);
     } else {
 #pragma unroll
@@ -276,10 +280,11 @@ template <int PREC> __device__ __forceinline__ unsigned vec_pack(float lo, float
         __half2 h = __floats2half2_rn(lo, hi);
         return *reinterpret_cast<unsigned *>(&h);
     } else if constexpr (PREC == F16C) {
-        bool o1, o2;
-        const unsigned a = f16c_bits(lo, o1), b = f16c_bits(hi, o2);
-        over |= o1 | o2;
-        return a | (b << 16);
+        // f16c_bits for two values, the range test on the OR of both rounded patterns
+        const unsigned ba = __float_as_uint(lo * F16C_ENCODE), bb = __float_as_uint(hi * F16C_ENCODE);
+        const unsigned ra = f16c_round(ba), rb = f16c_round(bb);
+        over |= ((ra | rb) & ~F16C_MAX_BITS) != 0;
+        return (ra & F16C_MAX_BITS) | ((ba >> 16) & 0x8000u) | ((rb & F16C_MAX_BITS) << 16) | (bb & 0x80000000u);
     } else {
         __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
         return *reinterpret_cast<unsigned *>(&h);
@@ -485,11 +490,22 @@ __global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::b
         }
     }
     __syncthreads();   // every read of this tile's old values happens before any write
-    if (!fluid) return;
-    if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, jy_prev_at(p, yi), p);
-    const auto m = collide<PREC>(f, p);
+    // collision layout with whole-warp tile rows: every thread takes part in the staged store
+    bool staged = false;
+    if constexpr (L == COLLISION) staged = (blockDim.x & 31u) == 0;
+    if (!staged && !fluid) return;
+    MomentsOf<PREC> m{};
+    if (fluid) {
+        if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, jy_prev_at(p, yi), p);
+        m = collide<PREC>(f, p);
+    }
+    if (staged) {
+        store_records_staged<PREC>(p, p.lat0, n, f, fluid);
+        if (!fluid) return;
+    } else {
 #pragma unroll
-    for (int d = 0; d < 9; ++d) st<PREC>(p.lat0, lidx<L>(n, d, p.N), d, f[d], p);
+        for (int d = 0; d < 9; ++d) st<PREC>(p.lat0, lidx<L>(n, d, p.N), d, f[d], p);
+    }
     if (lx == TW - 1 && tcx < p.n_col_bounds)
         for (int k = 0; k < 3; ++k) st<PREC>(p.halo_out, halo_col(p, tcx, yi, k), 3 * k + 2, f[3 * k + 2], p);
     if (lx == 0 && tcx > 0)
@@ -554,16 +570,12 @@ __global__ void k_nsol_even(StepParams p)
     emit_observables<PREC>(m, xi, yi, p);
 }
 
+// The odd-step gather of a fluid node: its own slots, a bounce-back link's value from the solid
+// neighbour's slot, ghost constants at the domain edge.
 template <int PREC, int L>
-__global__ void k_nsol_odd(StepParams p)
+__device__ __forceinline__ void nsol_odd_gather(CT<PREC> f[9], unsigned long long n, int xi, int yi, uint16_t lk,
+                                                const StepParams &p)
 {
-    const int xi = blockIdx.x * blockDim.x + threadIdx.x;
-    const int yi = blockIdx.y * blockDim.y + threadIdx.y;
-    if (xi >= p.W || yi >= p.H) return;
-    const unsigned long long n = (unsigned long long)xi + (unsigned long long)yi * p.P;
-    const uint16_t lk = link_at(p, n);
-    if (!(lk & LINK_FLUID)) return;
-    CT<PREC> f[9];
     if (lk == LINK_FLUID) {   // links carry LINK_EDGE on the domain edge
 #pragma unroll
         for (int d = 0; d < 9; ++d) f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N), d, p);
@@ -583,6 +595,39 @@ __global__ void k_nsol_odd(StepParams p)
             }
         }
     }
+}
+
+template <int PREC, int L>
+__global__ void k_nsol_odd(StepParams p)
+{
+    const int xi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int yi = blockIdx.y * blockDim.y + threadIdx.y;
+    if constexpr (L == COLLISION) {
+        // the node's own record, written reversed: whole-warp rows stage it (store_records_staged)
+        if ((blockDim.x & 31u) == 0) {
+            if (yi >= p.H || xi - (int)(threadIdx.x & 31u) >= p.P) return;   // warp-uniform
+            const bool in = xi < p.W;
+            const unsigned long long n = in ? (unsigned long long)xi + (unsigned long long)yi * p.P : 0;
+            const uint16_t lk = in ? link_at(p, n) : 0;
+            const bool fluid = (lk & LINK_FLUID) != 0;
+            CT<PREC> f[9];
+            MomentsOf<PREC> m{};
+            if (fluid) {
+                nsol_odd_gather<PREC, L>(f, n, xi, yi, lk, p);
+                if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, jy_prev_at(p, yi), p);
+                m = collide<PREC>(f, p);
+            }
+            store_records_staged<PREC, true>(p, p.lat0, n, f, fluid);
+            if (fluid) emit_observables<PREC>(m, xi, yi, p);
+            return;
+        }
+    }
+    if (xi >= p.W || yi >= p.H) return;
+    const unsigned long long n = (unsigned long long)xi + (unsigned long long)yi * p.P;
+    const uint16_t lk = link_at(p, n);
+    if (!(lk & LINK_FLUID)) return;
+    CT<PREC> f[9];
+    nsol_odd_gather<PREC, L>(f, n, xi, yi, lk, p);
     if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, jy_prev_at(p, yi), p);
     const auto m = collide<PREC>(f, p);
 #pragma unroll

@@ -25,7 +25,7 @@ constexpr float F16_SCALE = 4096.0f;
 // with a resolution of 2^-27.  IEEE half spends 5 exponent bits on a range the deviations never
 // use; this form gives that bit to the significand (relative rounding 2^-12 instead of 2^-11).
 // Decoding places the 15 magnitude bits in a float32 pattern and multiplies by 2^110; encoding
-// multiplies by 2^-110 and rounds the pattern to 11 significand bits (nearest, ties to even).
+// multiplies by 2^-110 and rounds the pattern to 11 significand bits (nearest, ties away from zero).
 constexpr float F16C_DECODE = 1.2980742146337069e33f;   // 2^110
 constexpr float F16C_ENCODE = 7.7037197775489434e-34f;  // 2^-110
 constexpr unsigned F16C_MAX_BITS = 0x7FFFu;            // largest magnitude pattern: (2 - 2^-11) * 2^-2
