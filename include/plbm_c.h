@@ -315,12 +315,15 @@ int plbm_nn_adam(float *w, const float *g, float *m, float *v, void *w_bf16, lon
                  float eps, int t, void *stream);
 /* Network input [N,H,W,C] (C >= 4): channel 0 the int8 solid mask, channels 1..3 the per-sample
  * scalars features[3n..3n+2] as constant planes, further channels zero. */
-/* 1 when plbm_nn_conv_fwd runs the shape (input channels Cin, output channels Cout) on the
- * tcgen05 tensor-core kernel: Cin a multiple of 32, Cout <= 128, W a multiple of 128 or a power of
- * two below 128 with H a multiple of 128 / W.  plbm_nn_conv_dgrad uses it with the two channel
- * counts exchanged; plbm_nn_conv_wgrad runs on tcgen05 when, in addition, Cin <= 128 and Cout is a
- * multiple of 32; other shapes run the mma.sync kernel. */
+/* 1 when plbm_nn_conv_fwd runs the shape (input channels Cin, output channels Cout) on tcgen05:
+ * W a multiple of 128 or a power of two below 128 with H a multiple of 128 / W, and either Cin a
+ * multiple of 32 with Cout <= 128 (TMA-fed kernel) or 9 * Cin <= 64 with Cout <= 64 (kernel whose
+ * threads write the im2col tile).  plbm_nn_conv_dgrad uses it with the two channel counts
+ * exchanged.  Other shapes run the mma.sync kernel. */
 int plbm_nn_conv_on_tensor_cores(int H, int W, int Cin, int Cout);
+/* 1 when plbm_nn_conv_wgrad runs the shape on tcgen05: the image tiling above, Cout <= 128, and
+ * either Cin and Cout multiples of 32 with Cin <= 128, or Cin <= 32. */
+int plbm_nn_wgrad_on_tensor_cores(int H, int W, int Cin, int Cout);
 /* Synchronises the device and reports whether a tensor-core convolution gave up on a wait (its
  * output is then invalid); clears the flag. */
 int plbm_nn_status(int *failed);

@@ -1,7 +1,8 @@
-// plbm_nn.cu — the convolutional neural operator's kernels: 3x3 "same" convolutions as implicit
-// GEMMs on the BF16 tensor cores (mma.sync m16n8k16, FP32 accumulate) for the forward pass, the
-// data gradient and the weight gradient; 2x2 average pooling, nearest upsampling, skip addition,
-// ReLU backward, the masked MSE loss and Adam.  Activations are NHWC bfloat16; weights are
+// plbm_nn.cu — the convolutional neural operator's kernels: the dispatch of the 3x3 "same"
+// convolutions (forward, data gradient, weight gradient) to the tcgen05 kernels of plbm_nn_tc.cu,
+// with an implicit GEMM on mma.sync m16n8k16 (BF16, FP32 accumulate) for the shapes those do not
+// tile; 2x2 average pooling, nearest upsampling, skip addition, ReLU backward, the masked MSE loss
+// and Adam.  Activations are NHWC bfloat16; weights are
 // W[co][k] with k = (ky * 3 + kx) * Cin + ci (bfloat16, FP32 master copy updated by Adam).
 //
 // No counterpart in the reference: this is the learned warm-start addition of the GB300 build.
@@ -19,6 +20,12 @@ int plbm_nn_tc_conv(const void *x, const void *w, const float *bias, void *y, in
 int plbm_nn_tc_flip(const void *w, void *wt, int Cin, int Cout, cudaStream_t s);
 bool plbm_nn_tc_wgrad_supported(int H, int W, int Cin, int Cout);
 int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int W, int Cin, int Cout, cudaStream_t s);
+bool plbm_nn_tc_small_supported(int H, int W, int Cin, int Cout);
+int plbm_nn_tc_small_conv(const void *x, const void *w, const float *bias, void *y, int N, int H, int W, int Cin,
+                          int Cout, int relu, cudaStream_t s);
+bool plbm_nn_tc_small_wgrad_supported(int H, int W, int Cin, int Cout);
+int plbm_nn_tc_small_wgrad(const void *x, const void *g, float *gw, int N, int H, int W, int Cin, int Cout,
+                           cudaStream_t s);
 
 namespace {
 
@@ -292,7 +299,158 @@ __global__ void k_assemble(const int8_t *mask, const float *features, __nv_bfloa
     }
 }
 
+// ---- 16-byte forms: eight channels per thread and 32-bit index arithmetic, for channel counts that
+// are multiples of 8 (every layer of the operator but its 4-channel input and 3-channel output) ----
+__device__ __forceinline__ void unpack8(const uint4 u, float f[8])
+{
+    const uint32_t w[4] = { u.x, u.y, u.z, u.w };
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        f[2 * k] = __uint_as_float(w[k] << 16);
+        f[2 * k + 1] = __uint_as_float(w[k] & 0xffff0000u);
+    }
+}
+__device__ __forceinline__ uint4 pack8(const float f[8])
+{
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        __nv_bfloat162 b = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+        w[k] = *reinterpret_cast<uint32_t *>(&b);
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// gb[c] += sum over the P pixels of g[p][c]: thread (pixel lane q, unit u) of a block of
+// R = blockDim.x / CU pixel lanes sums unit u of every (R * gridDim.x)-th pixel; the block's lanes
+// are then added per channel in shared memory, one atomic per channel and block.
+__global__ void k_bias_grad_v(const uint4 *g, float *gb, unsigned P, int CU)
+{
+    extern __shared__ float red[];
+    const int R = blockDim.x / CU, q = threadIdx.x / CU, u = threadIdx.x - q * CU;
+    float s[8] = { 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f };
+    if (q < R)
+        for (unsigned p = blockIdx.x * (unsigned)R + q; p < P; p += gridDim.x * (unsigned)R) {
+            float f[8];
+            unpack8(g[(size_t)p * CU + u], f);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) s[e] += f[e];
+        }
+    if (q < R)
+#pragma unroll
+        for (int e = 0; e < 8; ++e) red[threadIdx.x * 8 + e] = s[e];
+    __syncthreads();
+    for (int k = threadIdx.x; k < CU * 8; k += blockDim.x) {
+        float t = 0.f;
+        for (int qq = 0; qq < R; ++qq) t += red[qq * CU * 8 + k];
+        atomicAdd(&gb[k], t);
+    }
+}
+
+__global__ void k_relu_bwd_v(const uint4 *y, uint4 *g, unsigned n8)
+{
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += gridDim.x * blockDim.x) {
+        const uint4 yv = y[i];
+        uint4 gv = g[i];
+        uint32_t *gw = reinterpret_cast<uint32_t *>(&gv);
+        const uint32_t yw[4] = { yv.x, yv.y, yv.z, yv.w };
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {   // keep the gradient where y > 0 (a positive, non-NaN bfloat16)
+            const bool lo = __uint_as_float(yw[k] << 16) > 0.f, hi = __uint_as_float(yw[k] & 0xffff0000u) > 0.f;
+            gw[k] &= (lo ? 0x0000ffffu : 0u) | (hi ? 0xffff0000u : 0u);
+        }
+        g[i] = gv;
+    }
+}
+
+__global__ void k_add_v(const uint4 *a, const uint4 *b, uint4 *y, unsigned n8)
+{
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += gridDim.x * blockDim.x) {
+        float fa[8], fb[8];
+        unpack8(a[i], fa);
+        unpack8(b[i], fb);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) fa[e] += fb[e];
+        y[i] = pack8(fa);
+    }
+}
+
+// Output unit i of [N][H][W][CU] (H, W the output size) from input unit (n, yy / 2, xx / 2).
+__global__ void k_up2_v(const uint4 *x, uint4 *y, unsigned N, unsigned H, unsigned W, unsigned CU)
+{
+    const unsigned total = N * H * W * CU;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const unsigned cu = i % CU, t = i / CU, xx = t % W, t2 = t / W, yy = t2 % H, n = t2 / H;
+        y[i] = x[((n * (H / 2) + yy / 2) * (W / 2) + xx / 2) * CU + cu];
+    }
+}
+
+// Input-gradient unit i of [N][H][W][CU] (H, W the input size): the sum of its four output units.
+__global__ void k_up2_bwd_v(const uint4 *gy, uint4 *gx, unsigned N, unsigned H, unsigned W, unsigned CU)
+{
+    const unsigned total = N * H * W * CU;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const unsigned cu = i % CU, t = i / CU, x = t % W, t2 = t / W, yv = t2 % H, n = t2 / H;
+        const size_t b = ((size_t)(n * 2 * H + 2 * yv) * (2 * W) + 2 * x) * CU + cu, row = (size_t)2 * W * CU;
+        float s[8], f[8];
+        unpack8(gy[b], s);
+        unpack8(gy[b + CU], f);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[e] += f[e];
+        unpack8(gy[b + row], f);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[e] += f[e];
+        unpack8(gy[b + row + CU], f);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[e] += f[e];
+        gx[i] = pack8(s);
+    }
+}
+
+// Output unit i of [N][H/2][W/2][CU] (H, W the input size): the mean of its four input units.
+__global__ void k_pool2_v(const uint4 *x, uint4 *y, unsigned N, unsigned H, unsigned W, unsigned CU)
+{
+    const unsigned Ho = H / 2, Wo = W / 2, total = N * Ho * Wo * CU;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const unsigned cu = i % CU, t = i / CU, xo = t % Wo, t2 = t / Wo, yo = t2 % Ho, n = t2 / Ho;
+        const size_t b = ((size_t)(n * H + 2 * yo) * W + 2 * xo) * CU + cu, row = (size_t)W * CU;
+        float s[8], f[8];
+        unpack8(x[b], s);
+        unpack8(x[b + CU], f);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[e] += f[e];
+        unpack8(x[b + row], f);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[e] += f[e];
+        unpack8(x[b + row + CU], f);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[e] = 0.25f * (s[e] + f[e]);
+        y[i] = pack8(s);
+    }
+}
+
+// Input-gradient unit i of [N][H][W][CU] (H, W the input size): a quarter of its pooled unit.
+__global__ void k_pool2_bwd_v(const uint4 *gy, uint4 *gx, unsigned N, unsigned H, unsigned W, unsigned CU)
+{
+    const unsigned total = N * H * W * CU;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const unsigned cu = i % CU, t = i / CU, x = t % W, t2 = t / W, yv = t2 % H, n = t2 / H;
+        float f[8];
+        unpack8(gy[((size_t)(n * (H / 2) + yv / 2) * (W / 2) + x / 2) * CU + cu], f);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) f[e] *= 0.25f;
+        gx[i] = pack8(f);
+    }
+}
+
 int grid_for(long long n) { return (int)((n + 255) / 256 < 152 * 16 ? (n + 255) / 256 : 152 * 16); }
+
+// The 16-byte forms apply: C a multiple of 8, every pointer 16-byte aligned, units below 2^31.
+bool vec8(int C, long long elems, const void *a, const void *b = nullptr, const void *c = nullptr)
+{
+    const auto al = [](const void *p) { return p == nullptr || ((uintptr_t)p & 15u) == 0; };
+    return C % 8 == 0 && elems % 8 == 0 && elems / 8 < (1ll << 31) && al(a) && al(b) && al(c);
+}
 
 template <int MODE>
 int run_conv(ConvArgs a, cudaStream_t s)
@@ -316,6 +474,8 @@ int plbm_nn_conv_fwd(const void *x, const void *w, const float *bias, void *y, i
 {
     if (plbm_nn_tc_supported(H, W, Cin, Cout))
         return plbm_nn_tc_conv(x, w, bias, y, N, H, W, Cin, Cout, relu, (cudaStream_t)stream);
+    if (plbm_nn_tc_small_supported(H, W, Cin, Cout))
+        return plbm_nn_tc_small_conv(x, w, bias, y, N, H, W, Cin, Cout, relu, (cudaStream_t)stream);
     ConvArgs a{};
     a.x = (const __nv_bfloat16 *)x; a.w = (const __nv_bfloat16 *)w; a.bias = bias; a.y = (__nv_bfloat16 *)y;
     a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout; a.relu = relu;
@@ -325,9 +485,11 @@ int plbm_nn_conv_fwd(const void *x, const void *w, const float *bias, void *y, i
 
 int plbm_nn_conv_dgrad(const void *g, const void *w, void *gx, int N, int H, int W, int Cin, int Cout, void *stream)
 {
-    // gx = conv3x3(g, W') with W'[ci][tap][co] = W[co][8 - tap][ci]: the forward kernel on the
-    // tensor cores, with the re-laid-out weights in a buffer kept for the process
-    if (plbm_nn_tc_supported(H, W, Cout, Cin)) {
+    // gx = conv3x3(g, W') with W'[ci][tap][co] = W[co][8 - tap][ci]: a forward kernel on the
+    // tensor cores (the TMA one, or for a narrow gradient the one with thread-written tiles), with
+    // the re-laid-out weights in a buffer kept for the process
+    const bool tma = plbm_nn_tc_supported(H, W, Cout, Cin);
+    if (tma || plbm_nn_tc_small_supported(H, W, Cout, Cin)) {
         static std::mutex mu;
         static void *wt = nullptr;
         static size_t cap = 0;
@@ -342,7 +504,8 @@ int plbm_nn_conv_dgrad(const void *g, const void *w, void *gx, int N, int H, int
         }
         const int rc = plbm_nn_tc_flip(w, wt, Cin, Cout, (cudaStream_t)stream);
         if (rc != PLBM_OK) return rc;
-        return plbm_nn_tc_conv(g, wt, nullptr, gx, N, H, W, Cout, Cin, 0, (cudaStream_t)stream);
+        return tma ? plbm_nn_tc_conv(g, wt, nullptr, gx, N, H, W, Cout, Cin, 0, (cudaStream_t)stream)
+                   : plbm_nn_tc_small_conv(g, wt, nullptr, gx, N, H, W, Cout, Cin, 0, (cudaStream_t)stream);
     }
     ConvArgs a{};
     a.g = (const __nv_bfloat16 *)g; a.w = (const __nv_bfloat16 *)w; a.y = (__nv_bfloat16 *)gx;
@@ -357,6 +520,8 @@ int plbm_nn_conv_wgrad(const void *x, const void *g, float *gw, float *gb, int N
     int rc;
     if (plbm_nn_tc_wgrad_supported(H, W, Cin, Cout)) {
         rc = plbm_nn_tc_wgrad(x, g, gw, N, H, W, Cin, Cout, (cudaStream_t)stream);
+    } else if (plbm_nn_tc_small_wgrad_supported(H, W, Cin, Cout)) {
+        rc = plbm_nn_tc_small_wgrad(x, g, gw, N, H, W, Cin, Cout, (cudaStream_t)stream);
     } else {
         ConvArgs a{};
         a.x = (const __nv_bfloat16 *)x; a.g = (const __nv_bfloat16 *)g; a.gw = gw;
@@ -364,7 +529,14 @@ int plbm_nn_conv_wgrad(const void *x, const void *g, float *gw, float *gb, int N
         a.M = Cout; a.Ncols = 9 * Cin; a.K = N * H * W;
         rc = run_conv<WGRAD>(a, (cudaStream_t)stream);
     }
-    if (rc == PLBM_OK && gb) {
+    if (rc == PLBM_OK && gb && vec8(Cout, (long long)N * H * W * Cout, g)) {
+        const int CU = Cout / 8, threads = (256 / CU) * CU;
+        const long long P = (long long)N * H * W, R = threads / CU;
+        const int blocks = (int)((P + R - 1) / R < 152 * 4 ? (P + R - 1) / R : 152 * 4);
+        k_bias_grad_v<<<blocks, threads, threads * 8 * sizeof(float), (cudaStream_t)stream>>>(
+            (const uint4 *)g, gb, (unsigned)P, CU);
+        rc = cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+    } else if (rc == PLBM_OK && gb) {
         const long long P = (long long)N * H * W;
         const long long gx = (P + 7) / 8 < 1024 ? (P + 7) / 8 : 1024;
         dim3 grid((unsigned)gx, (unsigned)((Cout + 31) / 32));
@@ -376,12 +548,21 @@ int plbm_nn_conv_wgrad(const void *x, const void *g, float *gw, float *gb, int N
 
 int plbm_nn_relu_bwd(const void *y, void *g, long long n, void *stream)
 {
+    if (vec8(8, n, y, g)) {
+        k_relu_bwd_v<<<grid_for(n / 8), 256, 0, (cudaStream_t)stream>>>((const uint4 *)y, (uint4 *)g, (unsigned)(n / 8));
+        return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+    }
     k_relu_bwd<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)y, (__nv_bfloat16 *)g, n);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
 }
 
 int plbm_nn_pool2(const void *x, void *y, int N, int H, int W, int C, void *stream)
 {
+    if (vec8(C, (long long)N * H * W * C, x, y)) {
+        k_pool2_v<<<grid_for((long long)N * H * W * C / 32), 256, 0, (cudaStream_t)stream>>>(
+            (const uint4 *)x, (uint4 *)y, N, H, W, C / 8);
+        return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+    }
     k_pool2<<<grid_for((long long)N * H * W * C / 4), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)x,
                                                                                        (__nv_bfloat16 *)y, N, H, W, C);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
@@ -389,6 +570,11 @@ int plbm_nn_pool2(const void *x, void *y, int N, int H, int W, int C, void *stre
 
 int plbm_nn_pool2_bwd(const void *gy, void *gx, int N, int H, int W, int C, void *stream)
 {
+    if (vec8(C, (long long)N * H * W * C, gy, gx)) {
+        k_pool2_bwd_v<<<grid_for((long long)N * H * W * C / 8), 256, 0, (cudaStream_t)stream>>>(
+            (const uint4 *)gy, (uint4 *)gx, N, H, W, C / 8);
+        return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+    }
     k_pool2_bwd<<<grid_for((long long)N * H * W * C), 256, 0, (cudaStream_t)stream>>>(
         (const __nv_bfloat16 *)gy, (__nv_bfloat16 *)gx, N, H, W, C);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
@@ -396,6 +582,11 @@ int plbm_nn_pool2_bwd(const void *gy, void *gx, int N, int H, int W, int C, void
 
 int plbm_nn_up2(const void *x, void *y, int N, int H, int W, int C, void *stream)
 {
+    if (vec8(C, (long long)N * H * W * C, x, y)) {
+        k_up2_v<<<grid_for((long long)N * H * W * C / 8), 256, 0, (cudaStream_t)stream>>>(
+            (const uint4 *)x, (uint4 *)y, N, H, W, C / 8);
+        return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+    }
     k_up2<<<grid_for((long long)N * H * W * C), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)x,
                                                                                  (__nv_bfloat16 *)y, N, H, W, C);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
@@ -403,6 +594,11 @@ int plbm_nn_up2(const void *x, void *y, int N, int H, int W, int C, void *stream
 
 int plbm_nn_up2_bwd(const void *gy, void *gx, int N, int H, int W, int C, void *stream)
 {
+    if (vec8(C, (long long)N * H * W * C * 4, gy, gx)) {
+        k_up2_bwd_v<<<grid_for((long long)N * H * W * C / 8), 256, 0, (cudaStream_t)stream>>>(
+            (const uint4 *)gy, (uint4 *)gx, N, H, W, C / 8);
+        return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+    }
     k_up2_bwd<<<grid_for((long long)N * H * W * C), 256, 0, (cudaStream_t)stream>>>(
         (const __nv_bfloat16 *)gy, (__nv_bfloat16 *)gx, N, H, W, C);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
@@ -410,6 +606,11 @@ int plbm_nn_up2_bwd(const void *gy, void *gx, int N, int H, int W, int C, void *
 
 int plbm_nn_add(const void *a, const void *b, void *y, long long n, void *stream)
 {
+    if (vec8(8, n, a, b, y)) {
+        k_add_v<<<grid_for(n / 8), 256, 0, (cudaStream_t)stream>>>((const uint4 *)a, (const uint4 *)b, (uint4 *)y,
+                                                                  (unsigned)(n / 8));
+        return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+    }
     k_add<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)a, (const __nv_bfloat16 *)b,
                                                          (__nv_bfloat16 *)y, n);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;

@@ -100,6 +100,37 @@ __device__ __forceinline__ void umma_commit(unsigned bar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
+// Epilogue of one pixel: accumulator columns c0 .. c0 + 15 (FP32 bit patterns) plus the bias,
+// ReLU, rounded to BF16 and stored to out[c0 ..] for the channels below C; with C a multiple of 8,
+// as 16-byte stores of eight channels (a pixel row is 16-byte aligned then).
+__device__ __forceinline__ void store_row16(__nv_bfloat16 *out, int c0, int C, const unsigned v[16], const float *bias,
+                                            int relu)
+{
+    float f[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        f[j] = __uint_as_float(v[j]) + (bias && c0 + j < C ? bias[c0 + j] : 0.f);
+        if (relu) f[j] = fmaxf(f[j], 0.f);
+    }
+    if (C % 8 == 0) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (c0 + 8 * h >= C) break;
+            uint32_t q[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                __nv_bfloat162 b2 = __floats2bfloat162_rn(f[8 * h + 2 * e], f[8 * h + 2 * e + 1]);
+                q[e] = *reinterpret_cast<uint32_t *>(&b2);
+            }
+            *reinterpret_cast<uint4 *>(out + c0 + 8 * h) = make_uint4(q[0], q[1], q[2], q[3]);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            if (c0 + j < C) out[c0 + j] = __float2bfloat16_rn(f[j]);
+    }
+}
+
 struct TcArgs {
     __nv_bfloat16 *y;
     const float *bias;      // may be null
@@ -198,16 +229,7 @@ k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUte
                      : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         if (!valid || py >= a.H || px >= a.W) continue;
-        __nv_bfloat16 *out = a.y + (((size_t)n * a.H + py) * a.W + px) * a.Cout;
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            const int co = c0 + j;
-            if (co < a.Cout) {
-                float f = __uint_as_float(v[j]) + (a.bias ? a.bias[co] : 0.f);
-                if (a.relu) f = fmaxf(f, 0.f);
-                out[co] = __float2bfloat16_rn(f);
-            }
-        }
+        store_row16(a.y + (((size_t)n * a.H + py) * a.W + px) * a.Cout, c0, a.Cout, v, a.bias, a.relu);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -234,9 +256,10 @@ k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUte
 // MN-major ("transposed" in the instruction descriptor).  In that layout a swizzle atom is 8 K-rows
 // of 32 MN elements; the stride byte offset steps 8 K-rows (512 B) and the leading byte offset
 // steps 32 MN elements (the next 32-channel tile, WG_CHUNK bytes on).  M is Cout padded to 128
-// (TMA fills the channels past Cout with zeros); each of the CTA's taps accumulates N = Cin TMEM
+// with zero chunks; each of the CTA's taps accumulates N = Cin TMEM
 // columns.  A CTA walks (pixel tile, tap) pairs of its share of the pixels (split K, one CTA per
-// SM) and adds its partial sums to dW with FP32 atomics.
+// SM) and adds its partial sums to dW with FP32 atomics.  Only the Cout / 32 gradient chunks are
+// loaded; the chunks of the padding to 128 are zeroed once in every stage.
 constexpr int WG_M = 128;                          // TMEM lanes: Cout padded
 constexpr int WG_CHUNK = TC_BM * TC_KB * 2;        // one 128-pixel x 32-channel tile, 8 KB
 constexpr int WG_A_BYTES = (WG_M / TC_KB) * WG_CHUNK;   // 32 KB
@@ -291,6 +314,13 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
                      "r"(ncols) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
+    // the A chunks past Cout (the M padding to 128) are zeroed once and never loaded
+    const int achunks = (a.Cout + TC_KB - 1) / TC_KB;
+    for (int s = 0; s < a.stages; ++s) {
+        uint4 *z = reinterpret_cast<uint4 *>(smem + s * a.stage_bytes + achunks * WG_CHUNK);
+        for (int i = threadIdx.x; i < (WG_M / TC_KB - achunks) * WG_CHUNK / 16; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -316,8 +346,8 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
             const int dy = tap / 3 - 1, dx = tap % 3 - 1;
             unsigned char *st = smem + s * a.stage_bytes;
             const unsigned bar = smem_u32(&full[s]);
-            mbar_expect_tx(bar, (unsigned)WG_A_BYTES + (unsigned)a.b_bytes);
-            for (int c = 0; c < WG_M / TC_KB; ++c)
+            mbar_expect_tx(bar, (unsigned)(achunks * WG_CHUNK) + (unsigned)a.b_bytes);
+            for (int c = 0; c < achunks; ++c)
                 tma_load_4d(smem_u32(st + c * WG_CHUNK), &gmap, c * TC_KB, x0, y0, n, bar);
             for (int c = 0; c < kbx; ++c)
                 tma_load_4d(smem_u32(st + WG_A_BYTES + c * WG_CHUNK), &xmap, c * TC_KB, x0 + dx, y0 + dy, n, bar);
@@ -383,6 +413,318 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
     }
 }
 
+// ---- layers with a narrow side ----------------------------------------------------------------
+// A pixel of a tensor with fewer than 8 channels (the operator's 4-channel input, its 3-channel
+// output) is under TMA's 16-byte minimum row, so these layers' operands are written into shared
+// memory by the CTA's threads, in the layouts the TMA tiles above have (rows of 64 bytes, 16-byte
+// units swizzled in groups of 8 rows), and fed to the same tcgen05.mma forms:
+//  * forward (and, on the flipped weights, the input gradient) with 9 * Cin <= 64: M = 128 pixels,
+//    K = the (tap, ci) columns of the im2col tile padded to 32 or 64, N = Cout padded to 16;
+//  * weight gradient with Cin <= 32: M = Cout padded to 128 (the gradient tile), N = the 9 * Cin
+//    (tap, ci) columns of the im2col tile, K = the pixels, both MN-major as in k_wgrad_tc.
+constexpr int SM_BUILD = 128;      // threads of a CTA, all of which write operand tiles
+
+// Byte offset of 16-byte unit u (0..3) of row r in a 64-byte-swizzled tile whose base is 512-B
+// aligned: the unit index is XORed with bits 7..8 of the unswizzled offset, i.e. (r / 2) mod 4.
+__device__ __forceinline__ unsigned sw64_off(int r, int u) { return (unsigned)(r * 64 + ((u ^ ((r >> 1) & 3)) << 4)); }
+
+__device__ __forceinline__ unsigned short ld_bf16_bits(const __nv_bfloat16 *p)
+{
+    return __ldg(reinterpret_cast<const unsigned short *>(p));
+}
+
+// Unit U (columns 8U .. 8U + 7) of the im2col row of pixel (n, py, px): column c = tap * C + ch holds
+// src[n][py + s * (tap / 3 - 1)][px + s * (tap % 3 - 1)][ch] (zero outside the image and for
+// c >= 9 * C); s = 1 for the forward convolution.
+__device__ __forceinline__ uint4 im2col_unit(const __nv_bfloat16 *src, int C, int H, int W, int n, int py, int px,
+                                             int U)
+{
+    uint32_t v[4] = { 0u, 0u, 0u, 0u };
+    const int c0 = U * 8;
+    if (C % 8 == 0) {   // one tap, eight consecutive channels: a 16-byte load
+        const int tap = c0 / C, ch = c0 - tap * C;
+        const int sy = py + tap / 3 - 1, sx = px + tap % 3 - 1;
+        if (tap < 9 && sy >= 0 && sy < H && sx >= 0 && sx < W)
+            return __ldg(reinterpret_cast<const uint4 *>(src + (((size_t)n * H + sy) * W + sx) * C + ch));
+        return make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (C == 4) {       // two taps of four channels: two 8-byte loads
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int tap = 2 * U + h;
+            const int sy = py + tap / 3 - 1, sx = px + tap % 3 - 1;
+            if (tap < 9 && sy >= 0 && sy < H && sx >= 0 && sx < W) {
+                const uint2 q = __ldg(reinterpret_cast<const uint2 *>(src + (((size_t)n * H + sy) * W + sx) * 4));
+                v[2 * h] = q.x;
+                v[2 * h + 1] = q.y;
+            }
+        }
+        return make_uint4(v[0], v[1], v[2], v[3]);
+    }
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        const int c = c0 + e, tap = c / C, ch = c - tap * C;
+        const int sy = py + tap / 3 - 1, sx = px + tap % 3 - 1;
+        if (tap < 9 && sy >= 0 && sy < H && sx >= 0 && sx < W)
+            v[e >> 1] |= (uint32_t)ld_bf16_bits(src + (((size_t)n * H + sy) * W + sx) * C + ch) << (16 * (e & 1));
+    }
+    return make_uint4(v[0], v[1], v[2], v[3]);
+}
+
+// Unit U (channels 8U .. 8U + 7, zero past C) of pixel (n, py, px) of an NHWC tensor.
+__device__ __forceinline__ uint4 pixel_unit(const __nv_bfloat16 *src, int C, int H, int W, int n, int py, int px, int U)
+{
+    const __nv_bfloat16 *p = src + (((size_t)n * H + py) * W + px) * C;
+    if (C % 8 == 0) return __ldg(reinterpret_cast<const uint4 *>(p + U * 8));
+    uint32_t v[4] = { 0u, 0u, 0u, 0u };
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+        if (U * 8 + e < C) v[e >> 1] |= (uint32_t)ld_bf16_bits(p + U * 8 + e) << (16 * (e & 1));
+    return make_uint4(v[0], v[1], v[2], v[3]);
+}
+
+struct SmallArgs {
+    const __nv_bfloat16 *x;     // forward: input [N,H,W,Cin]; weight gradient: input
+    const __nv_bfloat16 *w;     // forward: weights [Cout][9 * Cin]
+    const __nv_bfloat16 *g;     // weight gradient: gradient of the output [N,H,W,Cout]
+    const float *bias;          // forward, may be null
+    __nv_bfloat16 *y;           // forward: output [N,H,W,Cout]
+    float *gw;                  // weight gradient: [Cout][9 * Cin], accumulated
+    int N, H, W, Cin, Cout, npad, relu;
+    int BW, BH, tiles_x, tiles_y;
+    int kchunks;                // forward: 32-column chunks of the im2col tile (1 or 2)
+    int bchunks;                // weight gradient: 32-column chunks of the im2col tile (<= 9)
+    int tiles_per_cta, total_tiles, stage_bytes;
+    int *err;
+};
+
+// Forward convolution of a narrow input: one 128-pixel tile per CTA; the threads write the im2col
+// tile (K-major: row = pixel, kchunks chunks of 32 columns) and the weights (row = output channel),
+// one thread issues kchunks * 2 MMAs (K = 16 each) into a TMEM accumulator of npad columns.
+__global__ void __launch_bounds__(SM_BUILD, 8) k_conv_small_tc(SmallArgs a)
+{
+    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+    unsigned char *smem = tc_smem_raw + ((1024 - (smem_u32(tc_smem_raw) & 1023)) & 1023);
+    unsigned char *As = smem, *Bs = smem + a.kchunks * WG_CHUNK;
+    unsigned long long *done = reinterpret_cast<unsigned long long *>(Bs + a.kchunks * a.npad * 64);
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(done + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned ncols = a.npad <= 32 ? 32u : (a.npad <= 64 ? 64u : 128u);
+    if (threadIdx.x == 0) {
+        mbar_init(smem_u32(done), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(ncols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    const int per_img = a.tiles_x * a.tiles_y;
+    const int n = blockIdx.x / per_img, t2 = blockIdx.x % per_img;
+    const int y0 = (t2 / a.tiles_x) * a.BH, x0 = (t2 % a.tiles_x) * a.BW;
+    {   // A: thread r writes row r (pixel r of the tile)
+        const int r = threadIdx.x, px = x0 + r % a.BW, py = y0 + r / a.BW;
+        for (int c = 0; c < a.kchunks; ++c) {
+            uint4 u[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) u[k] = im2col_unit(a.x, a.Cin, a.H, a.W, n, py, px, c * 4 + k);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) *reinterpret_cast<uint4 *>(As + c * WG_CHUNK + sw64_off(r, k)) = u[k];
+        }
+    }
+    const int K = 9 * a.Cin;
+    for (int i = threadIdx.x; i < a.kchunks * a.npad * 4; i += SM_BUILD) {   // B: row j = output channel j
+        const int c = i / (a.npad * 4), rem = i - c * a.npad * 4, j = rem >> 2, k = rem & 3;
+        uint32_t v[4] = { 0u, 0u, 0u, 0u };
+        if (j < a.Cout) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int col = c * 32 + k * 8 + e;
+                if (col < K) v[e >> 1] |= (uint32_t)ld_bf16_bits(a.w + (size_t)j * K + col) << (16 * (e & 1));
+            }
+        }
+        *reinterpret_cast<uint4 *>(Bs + c * a.npad * 64 + sw64_off(j, k)) = make_uint4(v[0], v[1], v[2], v[3]);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // the tiles are read by the tensor cores
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = *tmem_slot;
+    if (threadIdx.x == 0) {
+        const unsigned idesc = instr_desc(a.npad);
+        const unsigned abase = smem_u32(As), bbase = smem_u32(Bs);
+        for (int c = 0; c < a.kchunks; ++c)
+#pragma unroll
+            for (int k = 0; k < 2; ++k)
+                umma(tmem, smem_desc_sw64(abase + c * WG_CHUNK + 32 * k), smem_desc_sw64(bbase + c * a.npad * 64 + 32 * k),
+                     idesc, c > 0 || k > 0);
+        umma_commit(smem_u32(done));
+    }
+    const bool valid = mbar_wait(smem_u32(done), 0);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int row = warp * 32 + lane;
+    const int px = x0 + row % a.BW, py = y0 + row / a.BW;
+    for (int c0 = 0; c0 < a.npad; c0 += 16) {
+        unsigned v[16];
+        const unsigned taddr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0;
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                       "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                     : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (!valid || py >= a.H || px >= a.W) continue;
+        store_row16(a.y + (((size_t)n * a.H + py) * a.W + px) * a.Cout, c0, a.Cout, v, a.bias, a.relu);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && !valid) {
+        atomicExch(a.err, 1);
+        mbar_wait(smem_u32(done), 0);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+}
+
+// Weight gradient with a narrow side, as dW^T: M = the 9 * Cin (tap, ci) columns of the input's
+// im2col tile, N = Cout padded to 32 * gchunks, K = the pixels; both operands MN-major (a row is one
+// pixel holding 32 consecutive M or N elements, chunks 8 KB apart).  The M rows are covered by
+// tiles of four chunks (128 rows) starting at chunks 0, 4, ..., the last one moved back to end at
+// the last chunk (its rows already covered by the previous tile are computed twice and dropped),
+// so no zero chunks are multiplied once there are four.  A CTA walks its share of the 128-pixel
+// tiles through two stages: all threads load the tile's units (ten per thread in flight) and write
+// them swizzled, one thread issues the MMAs and releases the stage with tcgen05.commit, so writing
+// tile j + 1 overlaps the MMAs of tile j.  Four warps then read the accumulators (warp w: chunk
+// w of an M tile, lane = (tap, ci) column) and add them to dW[co][(tap, ci)] with FP32 atomics.
+constexpr int WS_THREADS = 256, WS_BATCH = 10;
+
+__device__ __forceinline__ int ws_mstart(int mt, int xchunks) { return xchunks > 4 ? min(4 * mt, xchunks - 4) : 0; }
+
+__global__ void __launch_bounds__(WS_THREADS, 1) k_wgrad_small_tc(SmallArgs a)
+{
+    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+    unsigned char *smem = tc_smem_raw + ((1024 - (smem_u32(tc_smem_raw) & 1023)) & 1023);
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + 2 * a.stage_bytes + WG_SLACK);
+    unsigned long long *empty = bars, *done = bars + 2;
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(bars + 3);
+    int *failed = reinterpret_cast<int *>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cols = 9 * a.Cin;                         // (tap, ci) columns
+    const int xchunks = a.bchunks, xalloc = max(xchunks, 4), mtiles = (xchunks + 3) / 4;
+    const int gchunks = (a.Cout + TC_KB - 1) / TC_KB, npad = gchunks * TC_KB;
+    const int used = mtiles * npad;
+    const unsigned ncols = used <= 32 ? 32u : used <= 64 ? 64u : used <= 128 ? 128u : used <= 256 ? 256u : 512u;
+    if (threadIdx.x == 0) {
+        mbar_init(smem_u32(&empty[0]), 1);
+        mbar_init(smem_u32(&empty[1]), 1);
+        mbar_init(smem_u32(done), 1);
+        *failed = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(ncols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    for (int i = threadIdx.x; i < 2 * a.stage_bytes / 16; i += WS_THREADS)   // units never written stay zero
+        reinterpret_cast<uint4 *>(smem)[i] = make_uint4(0u, 0u, 0u, 0u);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = *tmem_slot;
+
+    const int first = blockIdx.x * a.tiles_per_cta;
+    const int ntiles = max(0, min(a.tiles_per_cta, a.total_tiles - first));
+    const int per_img = a.tiles_x * a.tiles_y;
+    const int gunits = (a.Cout + 7) / 8, xunits = (cols + 7) / 8;
+    const int units = TC_BM * (gunits + xunits);        // (pixel, unit) pairs of a tile
+    const unsigned idesc = instr_desc_mn(npad);
+    for (int j = 0; j < ntiles; ++j) {
+        const int s = j & 1;
+        if (j >= 2 && threadIdx.x == 0 && !mbar_wait(smem_u32(&empty[s]), (unsigned)(((j >> 1) - 1) & 1))) *failed = 1;
+        __syncthreads();
+        if (*((volatile int *)failed)) break;
+        const int tile = first + j, n = tile / per_img, t2 = tile % per_img;
+        const int py0 = (t2 / a.tiles_x) * a.BH, px0 = (t2 % a.tiles_x) * a.BW;
+        unsigned char *Xs = smem + s * a.stage_bytes, *Gs = Xs + xalloc * WG_CHUNK;
+        for (int q0 = threadIdx.x; q0 < units; q0 += WS_THREADS * WS_BATCH) {
+            uint4 u[WS_BATCH];
+#pragma unroll
+            for (int k = 0; k < WS_BATCH; ++k) {   // unit q: pixel q % 128, unit q / 128 (gradient units first)
+                const int q = q0 + k * WS_THREADS;
+                if (q >= units) break;
+                const int r = q & (TC_BM - 1), U = q >> 7, py = py0 + r / a.BW, px = px0 + r % a.BW;
+                u[k] = U < gunits ? pixel_unit(a.g, a.Cout, a.H, a.W, n, py, px, U)
+                                  : im2col_unit(a.x, a.Cin, a.H, a.W, n, py, px, U - gunits);
+            }
+#pragma unroll
+            for (int k = 0; k < WS_BATCH; ++k) {
+                const int q = q0 + k * WS_THREADS;
+                if (q >= units) break;
+                const int r = q & (TC_BM - 1), U = q >> 7, V = U < gunits ? U : U - gunits;
+                unsigned char *base = U < gunits ? Gs : Xs;
+                *reinterpret_cast<uint4 *>(base + (V >> 2) * WG_CHUNK + sw64_off(r, V & 3)) = u[k];
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const unsigned xbase = smem_u32(Xs), gbase = smem_u32(Gs);
+#pragma unroll 1
+            for (int mt = 0; mt < mtiles; ++mt) {
+                const unsigned abase = xbase + (unsigned)(ws_mstart(mt, xchunks) * WG_CHUNK);
+#pragma unroll
+                for (int k = 0; k < TC_BM / 16; ++k)   // K = 16 pixels per MMA: two 8-row groups, 1 KB on
+                    umma(tmem + (unsigned)(mt * npad), smem_desc_mn_sw64(abase + 1024 * k, WG_CHUNK),
+                         smem_desc_mn_sw64(gbase + 1024 * k, WG_CHUNK), idesc, j > 0 || k > 0);
+            }
+            umma_commit(smem_u32(&empty[s]));
+        }
+    }
+    if (threadIdx.x == 0) umma_commit(smem_u32(done));   // arrives when every issued MMA has completed
+    if (!mbar_wait(smem_u32(done), 0)) *failed = 1;
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool valid = *((volatile int *)failed) == 0;
+    if (ntiles > 0 && warp < 4) {
+        for (int mt = 0; mt < mtiles; ++mt) {
+            const int chunk = ws_mstart(mt, xchunks) + warp;
+            if (chunk < 4 * mt || chunk >= xchunks) continue;   // computed by the previous tile / padding
+            const int col = chunk * TC_KB + lane;
+            for (int c0 = 0; c0 < npad; c0 += 16) {
+                unsigned v[16];
+                const unsigned taddr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(mt * npad + c0);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                               "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                             : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (!valid || col >= cols) continue;
+#pragma unroll
+                for (int e = 0; e < 16; ++e)
+                    if (c0 + e < a.Cout) atomicAdd(&a.gw[(size_t)(c0 + e) * cols + col], __uint_as_float(v[e]));
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && !valid) {
+        atomicExch(a.err, 1);
+        mbar_wait(smem_u32(done), 0);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+}
+
 // Wt[ci][tap][co] = W[co][8 - tap][ci]: the weights of the input-gradient convolution.
 __global__ void k_flip_weights(const __nv_bfloat16 *w, __nv_bfloat16 *wt, int Cin, int Cout)
 {
@@ -419,12 +761,18 @@ int *error_flag()
 
 // The tensor-core path covers Cin a multiple of 32, Cout <= 128, and images tiled exactly by
 // 128-pixel blocks (W a multiple of 128, or a power of two below it with H a multiple of 128 / W).
-bool plbm_nn_tc_supported(int H, int W, int Cin, int Cout)
+static bool tiles_exactly(int H, int W)
 {
-    if (Cin % TC_KB != 0 || Cin > 4096 || Cout < 1 || Cout > 128) return false;
+    if (H < 1 || W < 1) return false;
     if (W % TC_BM == 0) return true;
     if (TC_BM % W != 0) return false;
     return H % (TC_BM / W) == 0;
+}
+
+bool plbm_nn_tc_supported(int H, int W, int Cin, int Cout)
+{
+    if (Cin % TC_KB != 0 || Cin > 4096 || Cout < 1 || Cout > 128) return false;
+    return tiles_exactly(H, W);
 }
 
 // y = act(conv3x3(x, w) + bias) on the tensor cores; x, y NHWC BF16; w [Cout][9][Cin] BF16.
@@ -528,6 +876,69 @@ int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int 
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
 }
 
+// Forward convolution of a narrow input (9 * Cin <= 64, Cout <= 64: eight CTAs of at most 64 TMEM
+// columns share an SM) with the im2col tile written by the CTA's threads.
+bool plbm_nn_tc_small_supported(int H, int W, int Cin, int Cout)
+{
+    if (Cin < 1 || 9 * Cin > 2 * TC_KB || Cout < 1 || Cout > 64) return false;
+    return tiles_exactly(H, W);
+}
+
+int plbm_nn_tc_small_conv(const void *x, const void *w, const float *bias, void *y, int N, int H, int W, int Cin,
+                          int Cout, int relu, cudaStream_t s)
+{
+    int *err = error_flag();
+    if (!err) return PLBM_ERR_CUDA;
+    SmallArgs a{};
+    a.x = (const __nv_bfloat16 *)x; a.w = (const __nv_bfloat16 *)w; a.bias = bias; a.y = (__nv_bfloat16 *)y;
+    a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout; a.npad = (Cout + 15) / 16 * 16; a.relu = relu;
+    a.BW = W >= TC_BM ? TC_BM : W; a.BH = TC_BM / a.BW; a.tiles_x = W / a.BW; a.tiles_y = H / a.BH;
+    a.kchunks = (9 * Cin + TC_KB - 1) / TC_KB;
+    a.err = err;
+    const int smem = a.kchunks * (WG_CHUNK + a.npad * 64) + 1024 + 64;
+    k_conv_small_tc<<<N * a.tiles_x * a.tiles_y, SM_BUILD, smem, s>>>(a);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+// Weight gradient of a layer with Cin <= 32 (its 9 * Cin (tap, ci) columns in at most 9 chunks of 32)
+// and Cout <= 128, both operands written by the CTA's threads.
+bool plbm_nn_tc_small_wgrad_supported(int H, int W, int Cin, int Cout)
+{
+    if (Cin < 1 || Cin > TC_KB || Cout < 1 || Cout > WG_M) return false;
+    return tiles_exactly(H, W);
+}
+
+int plbm_nn_tc_small_wgrad(const void *x, const void *g, float *gw, int N, int H, int W, int Cin, int Cout,
+                           cudaStream_t s)
+{
+    int *err = error_flag();
+    if (!err) return PLBM_ERR_CUDA;
+    SmallArgs a{};
+    a.x = (const __nv_bfloat16 *)x; a.g = (const __nv_bfloat16 *)g; a.gw = gw;
+    a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout;
+    a.BW = W >= TC_BM ? TC_BM : W; a.BH = TC_BM / a.BW; a.tiles_x = W / a.BW; a.tiles_y = H / a.BH;
+    a.bchunks = (9 * Cin + TC_KB - 1) / TC_KB;
+    a.stage_bytes = (a.bchunks > 4 ? a.bchunks : 4) * WG_CHUNK + (Cout + TC_KB - 1) / TC_KB * WG_CHUNK;
+    a.err = err;
+    const int smem = 2 * a.stage_bytes + WG_SLACK + 1024 + 64;
+    static int attr_bytes = 0;
+    static std::mutex mu;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (smem > attr_bytes) {
+            if (cudaFuncSetAttribute(k_wgrad_small_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+                return PLBM_ERR_CUDA;
+            attr_bytes = smem;
+        }
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    a.total_tiles = N * a.tiles_x * a.tiles_y;
+    a.tiles_per_cta = (a.total_tiles + sms - 1) / sms;
+    k_wgrad_small_tc<<<(a.total_tiles + a.tiles_per_cta - 1) / a.tiles_per_cta, WS_THREADS, smem, s>>>(a);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
 int plbm_nn_tc_flip(const void *w, void *wt, int Cin, int Cout, cudaStream_t s)
 {
     const int total = Cout * 9 * Cin;
@@ -538,7 +949,12 @@ int plbm_nn_tc_flip(const void *w, void *wt, int Cin, int Cout, cudaStream_t s)
 
 extern "C" int plbm_nn_conv_on_tensor_cores(int H, int W, int Cin, int Cout)
 {
-    return plbm_nn_tc_supported(H, W, Cin, Cout) ? 1 : 0;
+    return plbm_nn_tc_supported(H, W, Cin, Cout) || plbm_nn_tc_small_supported(H, W, Cin, Cout) ? 1 : 0;
+}
+
+extern "C" int plbm_nn_wgrad_on_tensor_cores(int H, int W, int Cin, int Cout)
+{
+    return plbm_nn_tc_wgrad_supported(H, W, Cin, Cout) || plbm_nn_tc_small_wgrad_supported(H, W, Cin, Cout) ? 1 : 0;
 }
 
 extern "C" int plbm_nn_status(int *failed)

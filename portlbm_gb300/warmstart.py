@@ -110,18 +110,38 @@ def _ok(rc):
         raise RuntimeError(f"plbm_nn call failed ({rc})")
 
 
+PARAM_ALIGN = 128   # elements: every parameter segment starts 256-byte (FP32) / 128-byte (BF16) aligned
+
+
 class ConvLayer:
-    def __init__(self, cin, cout, relu, rng, torch):
+    """One 3x3 convolution's parameters: views into the operator's flat buffers (`Params`)."""
+
+    def __init__(self, cin, cout, relu, rng, params):
         self.cin, self.cout, self.relu = cin, cout, relu
         w = (rng.standard_normal((cout, 9 * cin)) * np.sqrt(2.0 / (9 * cin))).astype(np.float32)
-        self.w = torch.from_numpy(w).cuda()                        # FP32 master
-        assert self.w.dtype == torch.float32
-        self.wb = self.w.to(torch.bfloat16)                         # BF16 copy used by the kernels
-        self.b = torch.zeros(cout, dtype=torch.float32, device="cuda")
-        self.gw = torch.zeros_like(self.w)
-        self.gb = torch.zeros_like(self.b)
-        self.m = [torch.zeros_like(self.w), torch.zeros_like(self.b)]
-        self.v = [torch.zeros_like(self.w), torch.zeros_like(self.b)]
+        self.w, self.gw, self.m0, self.v0, self.wb = params.segment((cout, 9 * cin))   # FP32 master, BF16 copy
+        self.b, self.gb, self.m1, self.v1, _ = params.segment((cout,))
+        self.w.copy_(params.torch.from_numpy(w))
+        self.wb.copy_(self.w.to(params.torch.bfloat16))
+        self.m, self.v = [self.m0, self.m1], [self.v0, self.v1]
+
+
+class Params:
+    """Flat FP32 buffers for the weights and biases, their gradients and Adam's two moments, and a
+    BF16 copy of the weights: zeroing the gradients and the Adam update are one launch each."""
+
+    def __init__(self, sizes, torch):
+        self.torch = torch
+        self.total = sum(-(-int(np.prod(s)) // PARAM_ALIGN) * PARAM_ALIGN for s in sizes)
+        f32 = dict(dtype=torch.float32, device="cuda")
+        self.w, self.g, self.m, self.v = (torch.zeros(self.total, **f32) for _ in range(4))
+        self.wb = torch.zeros(self.total, dtype=torch.bfloat16, device="cuda")
+        self.off = 0
+
+    def segment(self, shape):
+        n = int(np.prod(shape))
+        a, self.off = self.off, self.off + -(-n // PARAM_ALIGN) * PARAM_ALIGN
+        return tuple(t[a:a + n].view(shape) for t in (self.w, self.g, self.m, self.v, self.wb))
 
 
 class NeuralOperator:
@@ -132,9 +152,13 @@ class NeuralOperator:
         self.torch = torch
         self.lib = _fns()
         rng = np.random.default_rng(seed)
-        self.enc = [ConvLayer(ci, co, True, rng, torch) for ci, co in ENC]
-        self.dec = [ConvLayer(ci, co, True, rng, torch) for ci, co in DEC]
-        self.head = ConvLayer(HEAD[0], HEAD[1], False, rng, torch)
+        shapes = []
+        for ci, co in ENC + DEC + [HEAD]:
+            shapes += [(co, 9 * ci), (co,)]
+        self.params = Params(shapes, torch)
+        self.enc = [ConvLayer(ci, co, True, rng, self.params) for ci, co in ENC]
+        self.dec = [ConvLayer(ci, co, True, rng, self.params) for ci, co in DEC]
+        self.head = ConvLayer(HEAD[0], HEAD[1], False, rng, self.params)
         self.layers = self.enc + self.dec + [self.head]
         self.norm = np.array([1.0, 1.0])          # std of t_rho and of t_j over the training set
         self.step_count = 0
@@ -240,19 +264,15 @@ class NeuralOperator:
             g = self._conv_bwd(self.enc[2 * lvl], xin, a[f"e{lvl}a"], ga, n, hh, ww, need_gx=lvl > 0)
 
     def zero_grad(self):
-        for layer in self.layers:
-            layer.gw.zero_()
-            layer.gb.zero_()
+        self.params.g.zero_()
 
     def adam(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        """One Adam update of every weight and bias (one launch over the flat buffers; the padding
+        between segments has zero gradients and stays zero)."""
         self.step_count += 1
-        for layer in self.layers:
-            _ok(self.lib.plbm_nn_adam(layer.w.data_ptr(), layer.gw.data_ptr(), layer.m[0].data_ptr(),
-                                      layer.v[0].data_ptr(), layer.wb.data_ptr(), layer.w.numel(), lr, b1, b2, eps,
-                                      self.step_count, None))
-            _ok(self.lib.plbm_nn_adam(layer.b.data_ptr(), layer.gb.data_ptr(), layer.m[1].data_ptr(),
-                                      layer.v[1].data_ptr(), None, layer.b.numel(), lr, b1, b2, eps, self.step_count,
-                                      None))
+        p = self.params
+        _ok(self.lib.plbm_nn_adam(p.w.data_ptr(), p.g.data_ptr(), p.m.data_ptr(), p.v.data_ptr(), p.wb.data_ptr(),
+                                  p.total, lr, b1, b2, eps, self.step_count, None))
 
     def assemble(self, masks, feats):
         """masks: [n,h,w] int8 device tensor; feats: n rows of `features` -> [n,h,w,4] bf16 input."""

@@ -126,6 +126,53 @@ def test_tensor_core_weight_gradient(plbm, n, h, w, cin, cout):
     assert lib.plbm_nn_status(ctypes.byref(failed)) == 0 and failed.value == 0
 
 
+@pytest.mark.parametrize("n,h,w,cin,cout", [(2, 8, 256, 4, 32), (2, 16, 64, 32, 3), (1, 16, 128, 3, 16),
+                                           (1, 8, 128, 5, 7), (2, 4, 32, 16, 8)])
+def test_narrow_layers_on_tensor_cores(plbm, n, h, w, cin, cout):
+    """Layers with a narrow side (the 4-channel input layer, the 3-channel head and other shapes
+    under TMA's 16-byte rows) on tcgen05 with thread-written im2col tiles: the forward pass for
+    9 * Cin <= 64, the input gradient for 9 * Cout <= 64 and the weight gradient for Cin <= 32,
+    against the CPU oracle; the weight gradient accumulates into a non-zero gw."""
+    import torch
+    lib = _lib(plbm)
+    lib.plbm_nn_conv_on_tensor_cores.argtypes = [ctypes.c_int] * 4
+    lib.plbm_nn_wgrad_on_tensor_cores.argtypes = [ctypes.c_int] * 4
+    lib.plbm_nn_status.argtypes = [ctypes.POINTER(ctypes.c_int)]
+    assert lib.plbm_nn_wgrad_on_tensor_cores(h, w, cin, cout) == 1
+    rng = np.random.default_rng(13 * cin + cout)
+    x = nn_ref.bf16_round(rng.standard_normal((n, h, w, cin)))
+    wt = nn_ref.bf16_round(rng.standard_normal((cout, 9 * cin)) / np.sqrt(9 * cin))
+    b = rng.standard_normal(cout).astype(np.float32)
+    g = nn_ref.bf16_round(rng.standard_normal((n, h, w, cout)))
+    xd, wd, gd, bd = _bf(x), _bf(wt), _bf(g), torch.tensor(b).cuda()
+    if 9 * cin <= 64:
+        assert lib.plbm_nn_conv_on_tensor_cores(h, w, cin, cout) == 1
+        y = torch.empty((n, h, w, cout), dtype=torch.bfloat16, device="cuda")
+        for relu in (0, 1):
+            assert lib.plbm_nn_conv_fwd(xd.data_ptr(), wd.data_ptr(), bd.data_ptr(), y.data_ptr(), n, h, w, cin,
+                                        cout, relu, None) == 0
+            torch.cuda.synchronize()
+            _close(_np(y), nn_ref.conv_fwd(x, wt, b.astype(np.float64), bool(relu)))
+    if 9 * cout <= 64:
+        assert lib.plbm_nn_conv_on_tensor_cores(h, w, cout, cin) == 1
+        gx = torch.empty((n, h, w, cin), dtype=torch.bfloat16, device="cuda")
+        assert lib.plbm_nn_conv_dgrad(gd.data_ptr(), wd.data_ptr(), gx.data_ptr(), n, h, w, cin, cout, None) == 0
+        torch.cuda.synchronize()
+        _close(_np(gx), nn_ref.conv_dgrad(g, wt, cin))
+    rgw, rgb = nn_ref.conv_wgrad(x, g)
+    start = rng.standard_normal((cout, 9 * cin)).astype(np.float32)
+    gw = torch.tensor(start).cuda()
+    gb = torch.zeros(cout, dtype=torch.float32, device="cuda")
+    assert lib.plbm_nn_conv_wgrad(xd.data_ptr(), gd.data_ptr(), gw.data_ptr(), gb.data_ptr(), n, h, w, cin, cout,
+                                  None) == 0
+    torch.cuda.synchronize()
+    got = gw.cpu().numpy().astype(np.float64) - start
+    assert np.max(np.abs(got - rgw)) <= 1e-3 * np.max(np.abs(rgw)), np.max(np.abs(got - rgw))
+    assert np.max(np.abs(_np(gb) - rgb)) <= 1e-2 * np.max(np.abs(rgb)) + 1e-2
+    failed = ctypes.c_int(-1)
+    assert lib.plbm_nn_status(ctypes.byref(failed)) == 0 and failed.value == 0
+
+
 def test_pool_and_upsample(plbm):
     import torch
     lib = _lib(plbm)

@@ -91,18 +91,23 @@ def test_state_difference_over_fluid_nodes():
 
 @pytest.mark.parametrize("h,w", [(256, 256), (256, 1024)])
 def test_tensor_core_dispatch_covers_the_network(plbm, h, w):
-    """Every convolution of the operator runs on tcgen05 except the 4-channel input layer; so does
-    every input gradient except the head's (3 channels in): the host-side dispatch predicate over
-    each layer's resolution and channel counts."""
+    """Every convolution of the operator, every input gradient and every weight gradient runs on
+    tcgen05 (the TMA-fed kernels, or for the 4-channel input layer and the 3-channel head the
+    kernels whose threads write the im2col tiles): the host-side dispatch predicates over each
+    layer's resolution and channel counts."""
     import ctypes
     lib = plbm.load_library()
     lib.plbm_nn_conv_on_tensor_cores.argtypes = [ctypes.c_int] * 4
-    tc = lib.plbm_nn_conv_on_tensor_cores
+    lib.plbm_nn_wgrad_on_tensor_cores.argtypes = [ctypes.c_int] * 4
+    tc, tcw = lib.plbm_nn_conv_on_tensor_cores, lib.plbm_nn_wgrad_on_tensor_cores
     layers = [(lvl, ci, co) for lvl in range(5) for ci, co in ws.ENC[2 * lvl:2 * lvl + 2]]
     layers += [(lvl, ci, co) for k, lvl in enumerate((3, 2, 1, 0)) for ci, co in ws.DEC[2 * k:2 * k + 2]]
     layers.append((0,) + tuple(ws.HEAD))
     for lvl, ci, co in layers:
         hh, ww = h >> lvl, w >> lvl
-        assert tc(hh, ww, ci, co) == (0 if ci == ws.C_IN else 1), (lvl, ci, co)
-        if ci != ws.C_IN:   # the input gradient: the same kernel with channels swapped
-            assert tc(hh, ww, co, ci) == (0 if co == ws.HEAD[1] else 1), (lvl, co, ci)
+        assert tc(hh, ww, ci, co) == 1, (lvl, ci, co)
+        assert tcw(hh, ww, ci, co) == 1, (lvl, ci, co)
+        if ci != ws.C_IN:   # the input gradient: a forward kernel with the channels swapped
+            assert tc(hh, ww, co, ci) == 1, (lvl, co, ci)
+    # shapes neither tcgen05 kernel tiles fall back to mma.sync
+    assert tc(16, 24, 4, 32) == 0 and tc(256, 256, 16, 32) == 0 and tcw(256, 256, 48, 32) == 0
