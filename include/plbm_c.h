@@ -322,7 +322,8 @@ int plbm_nn_adam(float *w, const float *g, float *m, float *v, void *w_bf16, lon
  * exchanged.  Other shapes run the mma.sync kernel. */
 int plbm_nn_conv_on_tensor_cores(int H, int W, int Cin, int Cout);
 /* 1 when plbm_nn_conv_wgrad runs the shape on tcgen05: the image tiling above, Cout <= 128, and
- * either Cin and Cout multiples of 32 with Cin <= 128, or Cin <= 32. */
+ * either Cin a multiple of 32 up to 128 (TMA-fed input tiles) or Cin <= 32 (im2col tiles written by
+ * the CTA's threads). */
 int plbm_nn_wgrad_on_tensor_cores(int H, int W, int Cin, int Cout);
 /* Synchronises the device and reports whether a tensor-core convolution gave up on a wait (its
  * output is then invalid); clears the flag. */

@@ -22,6 +22,7 @@
 #include <cudaTypedefs.h>
 
 #include <cstdint>
+#include <cstring>
 #include <mutex>
 
 namespace {
@@ -249,29 +250,34 @@ k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUte
 }
 
 // ---- weight gradient ------------------------------------------------------------------------
-// dW[co][tap][ci] += sum over pixels p of g[p][co] * x[p + offset(tap)][ci]: a GEMM with M = Cout,
-// N = Cin per tap and K = the pixels.  Both operands arrive as TMA tiles of 128 pixels x 32
-// channels (64-byte rows, 64-byte swizzle), exactly the tiles of the forward kernel: a row is one
-// pixel, i.e. one K index, holding 32 consecutive M (or N) elements, so both are fed to tcgen05.mma
-// MN-major ("transposed" in the instruction descriptor).  In that layout a swizzle atom is 8 K-rows
-// of 32 MN elements; the stride byte offset steps 8 K-rows (512 B) and the leading byte offset
-// steps 32 MN elements (the next 32-channel tile, WG_CHUNK bytes on).  M is Cout padded to 128
-// with zero chunks; each of the CTA's taps accumulates N = Cin TMEM
-// columns.  A CTA walks (pixel tile, tap) pairs of its share of the pixels (split K, one CTA per
-// SM) and adds its partial sums to dW with FP32 atomics.  Only the Cout / 32 gradient chunks are
-// loaded; the chunks of the padding to 128 are zeroed once in every stage.
-constexpr int WG_M = 128;                          // TMEM lanes: Cout padded
+// dW[co][tap][ci] += sum over pixels p of g[p][co] * x[p + offset(tap)][ci], computed as its
+// transpose: a GEMM with M = the (tap, ci) rows, N = Cout and K = the pixels.  A stage holds, for
+// one 128-pixel tile, the shifted input tiles of TG taps (TG * Cin / 32 TMA tiles of 128 pixels x 32
+// channels, 64-byte rows with the 64-byte swizzle, exactly the tiles of the forward kernel) and the
+// tile's output gradient (Cout / 32 such tiles, or for Cout < 32 written by two warps).  A row of
+// either is one pixel, i.e. one K index, holding 32 consecutive M (or N) elements, so both are
+// fed to tcgen05.mma MN-major ("transposed" in the instruction descriptor): a swizzle atom is 8
+// K-rows of 32 MN elements, the stride byte offset steps 8 K-rows (512 B) and the leading byte
+// offset the next 32-element tile (WG_CHUNK bytes on).  The stage's input tiles are covered by M
+// tiles of four (128 rows) starting at tiles 0, 4, ..., the last moved back to end at the last one
+// (rows it shares with the previous M tile are computed twice and dropped), so one load of the
+// gradient serves every tap of the stage and no zero padding is multiplied.  A CTA walks its share
+// of the pixel tiles (split K, one CTA per SM, 2-4 stages of 64-104 KB in flight) for the taps of
+// its group (blockIdx.y) and adds its partial sums to dW with FP32 atomics.
+constexpr int WG_M = 128;                          // rows of an M tile (TMEM lanes)
 constexpr int WG_CHUNK = TC_BM * TC_KB * 2;        // one 128-pixel x 32-channel tile, 8 KB
-constexpr int WG_A_BYTES = (WG_M / TC_KB) * WG_CHUNK;   // 32 KB
 constexpr int WG_SLACK = 16384;                    // keeps any reading of the descriptors inside the allocation
 
 struct WgArgs {
     float *gw;
+    const __nv_bfloat16 *g;   // the output gradient, read by threads when Cout is not a multiple of 32
     int N, H, W, Cin, Cout;
     int BW, BH, tiles_x, tiles_y;
-    int ntaps;              // taps per CTA (3 or 9); blockIdx.y selects the group
+    int ntaps;              // taps of a CTA (9 or 3; blockIdx.y selects the group)
+    int tg;                 // taps per stage (a divisor of ntaps)
     int tiles_per_cta, total_tiles;
-    int b_bytes, stage_bytes, stages;
+    int xchunks, gchunks, stage_bytes, stages;
+    int g_tma;              // 1: the gradient tiles come by TMA
     int *err;
 };
 
@@ -290,6 +296,30 @@ __device__ __forceinline__ unsigned instr_desc_mn(int n)
            ((unsigned)(WG_M >> 4) << 24);
 }
 
+// First 32-row tile of M tile mt over `chunks` tiles (the last M tile ends at the last tile).
+__device__ __forceinline__ int ws_mstart(int mt, int chunks) { return chunks > 4 ? min(4 * mt, chunks - 4) : 0; }
+
+// Byte offset of 16-byte unit u (0..3) of row r in a 64-byte-swizzled tile whose base is 512-B
+// aligned: the unit index is XORed with bits 7..8 of the unswizzled offset, i.e. (r / 2) mod 4.
+__device__ __forceinline__ unsigned sw64_off(int r, int u) { return (unsigned)(r * 64 + ((u ^ ((r >> 1) & 3)) << 4)); }
+
+__device__ __forceinline__ unsigned short ld_bf16_bits(const __nv_bfloat16 *p)
+{
+    return __ldg(reinterpret_cast<const unsigned short *>(p));
+}
+
+// Unit U (channels 8U .. 8U + 7, zero past C) of pixel (n, py, px) of an NHWC tensor.
+__device__ __forceinline__ uint4 pixel_unit(const __nv_bfloat16 *src, int C, int H, int W, int n, int py, int px, int U)
+{
+    const __nv_bfloat16 *p = src + (((size_t)n * H + py) * W + px) * C;
+    if (C % 8 == 0) return __ldg(reinterpret_cast<const uint4 *>(p + U * 8));
+    uint32_t v[4] = { 0u, 0u, 0u, 0u };
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+        if (U * 8 + e < C) v[e >> 1] |= (uint32_t)ld_bf16_bits(p + U * 8 + e) << (16 * (e & 1));
+    return make_uint4(v[0], v[1], v[2], v[3]);
+}
+
 __global__ void __launch_bounds__(128, 1)
 k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap gmap, WgArgs a)
 {
@@ -301,10 +331,15 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
     int *counts = reinterpret_cast<int *>(tmem_slot + 1);   // [0] issued, [1] consumed, [2] failed
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int cols = a.ntaps * a.Cin;
-    const unsigned ncols = cols <= 32 ? 32u : cols <= 64 ? 64u : cols <= 128 ? 128u : cols <= 256 ? 256u : 512u;
+    const int npad = a.gchunks * TC_KB, mtiles = (a.xchunks + 3) / 4, blocks = a.ntaps / a.tg;
+    const int used = blocks * mtiles * npad;
+    const unsigned ncols = used <= 32 ? 32u : used <= 64 ? 64u : used <= 128 ? 128u : used <= 256 ? 256u : 512u;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < a.stages; ++s) { mbar_init(smem_u32(&full[s]), 1); mbar_init(smem_u32(&empty[s]), 1); }
+        // full: the TMA producer's arrive (with the byte count), plus the two writer warps'
+        for (int s = 0; s < a.stages; ++s) {
+            mbar_init(smem_u32(&full[s]), a.g_tma ? 1 : 3);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
         mbar_init(smem_u32(done), 1);
         counts[0] = counts[1] = counts[2] = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -314,13 +349,13 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
                      "r"(ncols) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    // the A chunks past Cout (the M padding to 128) are zeroed once and never loaded
-    const int achunks = (a.Cout + TC_KB - 1) / TC_KB;
-    for (int s = 0; s < a.stages; ++s) {
-        uint4 *z = reinterpret_cast<uint4 *>(smem + s * a.stage_bytes + achunks * WG_CHUNK);
-        for (int i = threadIdx.x; i < (WG_M / TC_KB - achunks) * WG_CHUNK / 16; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (!a.g_tma) {   // the gradient units the writers never touch stay zero
+        for (int s = 0; s < a.stages; ++s) {
+            uint4 *z = reinterpret_cast<uint4 *>(smem + s * a.stage_bytes + a.xchunks * WG_CHUNK);
+            for (int i = threadIdx.x; i < a.gchunks * WG_CHUNK / 16; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -329,32 +364,36 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
     const int tap0 = blockIdx.y * a.ntaps;
     const int first = blockIdx.x * a.tiles_per_cta;
     const int ntiles = max(0, min(a.tiles_per_cta, a.total_tiles - first));
-    const int iters = ntiles * a.ntaps;
+    const int iters = ntiles * blocks;
     const int per_img = a.tiles_x * a.tiles_y;
     const int kbx = a.Cin / TC_KB;
 
-    if (warp == 0 && lane == 0) {              // producer: TMA loads of the g tile and the shifted x tile
+    if (warp == 0 && lane == 0) {              // producer: TMA loads of the shifted x tiles and the g tiles
+        const unsigned bytes = (unsigned)((a.xchunks + (a.g_tma ? a.gchunks : 0)) * WG_CHUNK);
         for (int it = 0; it < iters; ++it) {
             const int s = it % a.stages;
             if (it >= a.stages && !mbar_wait(smem_u32(&empty[s]), (unsigned)((it / a.stages - 1) & 1))) {
                 counts[2] = 1;
                 break;
             }
-            const int tile = first + it / a.ntaps, tap = tap0 + it % a.ntaps;
+            const int tile = first + it / blocks, b = it % blocks;
             const int n = tile / per_img, t2 = tile % per_img;
             const int y0 = (t2 / a.tiles_x) * a.BH, x0 = (t2 % a.tiles_x) * a.BW;
-            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
             unsigned char *st = smem + s * a.stage_bytes;
             const unsigned bar = smem_u32(&full[s]);
-            mbar_expect_tx(bar, (unsigned)(achunks * WG_CHUNK) + (unsigned)a.b_bytes);
-            for (int c = 0; c < achunks; ++c)
-                tma_load_4d(smem_u32(st + c * WG_CHUNK), &gmap, c * TC_KB, x0, y0, n, bar);
-            for (int c = 0; c < kbx; ++c)
-                tma_load_4d(smem_u32(st + WG_A_BYTES + c * WG_CHUNK), &xmap, c * TC_KB, x0 + dx, y0 + dy, n, bar);
+            mbar_expect_tx(bar, bytes);
+            for (int t = 0; t < a.tg; ++t) {
+                const int tap = tap0 + b * a.tg + t, dy = tap / 3 - 1, dx = tap % 3 - 1;
+                for (int c = 0; c < kbx; ++c)
+                    tma_load_4d(smem_u32(st + (t * kbx + c) * WG_CHUNK), &xmap, c * TC_KB, x0 + dx, y0 + dy, n, bar);
+            }
+            if (a.g_tma)
+                for (int c = 0; c < a.gchunks; ++c)
+                    tma_load_4d(smem_u32(st + (a.xchunks + c) * WG_CHUNK), &gmap, c * TC_KB, x0, y0, n, bar);
             counts[0] = it + 1;
         }
     } else if (warp == 1 && lane == 0) {       // MMA issuer
-        const unsigned idesc = instr_desc_mn(a.Cin);
+        const unsigned idesc = instr_desc_mn(npad);
         int it = 0;
         for (; it < iters; ++it) {
             const int s = it % a.stages;
@@ -363,40 +402,70 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const unsigned abase = smem_u32(smem + s * a.stage_bytes), bbase = abase + WG_A_BYTES;
-            const unsigned dcol = tmem + (unsigned)((it % a.ntaps) * a.Cin);
-            const bool first_tile = it < a.ntaps;
+            const unsigned xbase = smem_u32(smem + s * a.stage_bytes), gbase = xbase + (unsigned)(a.xchunks * WG_CHUNK);
+            const int b = it % blocks;
+            const bool first_tile = it < blocks;
+            for (int mt = 0; mt < mtiles; ++mt) {
+                const unsigned abase = xbase + (unsigned)(ws_mstart(mt, a.xchunks) * WG_CHUNK);
+                const unsigned dcol = tmem + (unsigned)((b * mtiles + mt) * npad);
 #pragma unroll
-            for (int k = 0; k < TC_BM / 16; ++k)   // K = 16 pixels per MMA: two 8-row groups, 1 KB on
-                umma(dcol, smem_desc_mn_sw64(abase + 1024 * k, WG_CHUNK), smem_desc_mn_sw64(bbase + 1024 * k, WG_CHUNK),
-                     idesc, !(first_tile && k == 0));
+                for (int k = 0; k < TC_BM / 16; ++k)   // K = 16 pixels per MMA: two 8-row groups, 1 KB on
+                    umma(dcol, smem_desc_mn_sw64(abase + 1024 * k, WG_CHUNK), smem_desc_mn_sw64(gbase + 1024 * k, WG_CHUNK),
+                         idesc, !(first_tile && k == 0));
+            }
             umma_commit(smem_u32(&empty[s]));
             counts[1] = it + 1;
         }
         umma_commit(smem_u32(done));
+    } else if (warp >= 2 && !a.g_tma) {        // writers of the narrow gradient tiles
+        const int gunits = (a.Cout + 7) / 8;
+        for (int it = 0; it < iters; ++it) {
+            const int s = it % a.stages;
+            bool ok = true;
+            if (lane == 0 && it >= a.stages) ok = mbar_wait(smem_u32(&empty[s]), (unsigned)((it / a.stages - 1) & 1));
+            if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) {
+                if (lane == 0) counts[2] = 1;
+                break;
+            }
+            const int tile = first + it / blocks, n = tile / per_img, t2 = tile % per_img;
+            const int y0 = (t2 / a.tiles_x) * a.BH, x0 = (t2 % a.tiles_x) * a.BW;
+            unsigned char *gs = smem + s * a.stage_bytes + a.xchunks * WG_CHUNK;
+            for (int q = threadIdx.x - 64; q < TC_BM * gunits; q += 64) {
+                const int r = q & (TC_BM - 1), U = q >> 7;
+                *reinterpret_cast<uint4 *>(gs + (U >> 2) * WG_CHUNK + sw64_off(r, U & 3)) =
+                    pixel_unit(a.g, a.Cout, a.H, a.W, n, y0 + r / a.BW, x0 + r % a.BW, U);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full[s])) : "memory");
+        }
     }
     if (!mbar_wait(smem_u32(done), 0)) counts[2] = 1;
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const bool valid = *((volatile int *)&counts[2]) == 0;
-    const int co = warp * 32 + lane;
     if (iters > 0) {
-        for (int c0 = 0; c0 < cols; c0 += 16) {
-            unsigned v[16];
-            const unsigned taddr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0;
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
-                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                           "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-                         : "r"(taddr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (!valid || co >= a.Cout) continue;
+        const int rows = 9 * a.Cin;
+        for (int b = 0; b < blocks; ++b)
+            for (int mt = 0; mt < mtiles; ++mt) {
+                const int chunk = ws_mstart(mt, a.xchunks) + warp;   // warp w reads rows 32w .. 32w + 31
+                if (chunk < 4 * mt || chunk >= a.xchunks) continue;   // computed by the previous M tile
+                const int tap = tap0 + b * a.tg + chunk / kbx, row = tap * a.Cin + (chunk % kbx) * TC_KB + lane;
+                for (int c0 = 0; c0 < npad; c0 += 16) {
+                    unsigned v[16];
+                    const unsigned taddr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)((b * mtiles + mt) * npad + c0);
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                                   "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                                 : "r"(taddr));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    if (!valid) continue;
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int col = c0 + j, t = col / a.Cin, ci = col % a.Cin;
-                atomicAdd(&a.gw[(size_t)co * 9 * a.Cin + (size_t)(tap0 + t) * a.Cin + ci], __uint_as_float(v[j]));
+                    for (int e = 0; e < 16; ++e)
+                        if (c0 + e < a.Cout) atomicAdd(&a.gw[(size_t)(c0 + e) * rows + row], __uint_as_float(v[e]));
+                }
             }
-        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -423,15 +492,6 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
 //  * weight gradient with Cin <= 32: M = Cout padded to 128 (the gradient tile), N = the 9 * Cin
 //    (tap, ci) columns of the im2col tile, K = the pixels, both MN-major as in k_wgrad_tc.
 constexpr int SM_BUILD = 128;      // threads of a CTA, all of which write operand tiles
-
-// Byte offset of 16-byte unit u (0..3) of row r in a 64-byte-swizzled tile whose base is 512-B
-// aligned: the unit index is XORed with bits 7..8 of the unswizzled offset, i.e. (r / 2) mod 4.
-__device__ __forceinline__ unsigned sw64_off(int r, int u) { return (unsigned)(r * 64 + ((u ^ ((r >> 1) & 3)) << 4)); }
-
-__device__ __forceinline__ unsigned short ld_bf16_bits(const __nv_bfloat16 *p)
-{
-    return __ldg(reinterpret_cast<const unsigned short *>(p));
-}
 
 // Unit U (columns 8U .. 8U + 7) of the im2col row of pixel (n, py, px): column c = tap * C + ch holds
 // src[n][py + s * (tap / 3 - 1)][px + s * (tap % 3 - 1)][ch] (zero outside the image and for
@@ -468,18 +528,6 @@ __device__ __forceinline__ uint4 im2col_unit(const __nv_bfloat16 *src, int C, in
         if (tap < 9 && sy >= 0 && sy < H && sx >= 0 && sx < W)
             v[e >> 1] |= (uint32_t)ld_bf16_bits(src + (((size_t)n * H + sy) * W + sx) * C + ch) << (16 * (e & 1));
     }
-    return make_uint4(v[0], v[1], v[2], v[3]);
-}
-
-// Unit U (channels 8U .. 8U + 7, zero past C) of pixel (n, py, px) of an NHWC tensor.
-__device__ __forceinline__ uint4 pixel_unit(const __nv_bfloat16 *src, int C, int H, int W, int n, int py, int px, int U)
-{
-    const __nv_bfloat16 *p = src + (((size_t)n * H + py) * W + px) * C;
-    if (C % 8 == 0) return __ldg(reinterpret_cast<const uint4 *>(p + U * 8));
-    uint32_t v[4] = { 0u, 0u, 0u, 0u };
-#pragma unroll
-    for (int e = 0; e < 8; ++e)
-        if (U * 8 + e < C) v[e >> 1] |= (uint32_t)ld_bf16_bits(p + U * 8 + e) << (16 * (e & 1));
     return make_uint4(v[0], v[1], v[2], v[3]);
 }
 
@@ -600,8 +648,6 @@ __global__ void __launch_bounds__(SM_BUILD, 8) k_conv_small_tc(SmallArgs a)
 // tile j + 1 overlaps the MMAs of tile j.  Four warps then read the accumulators (warp w: chunk
 // w of an M tile, lane = (tap, ci) column) and add them to dW[co][(tap, ci)] with FP32 atomics.
 constexpr int WS_THREADS = 256, WS_BATCH = 10;
-
-__device__ __forceinline__ int ws_mstart(int mt, int xchunks) { return xchunks > 4 ? min(4 * mt, xchunks - 4) : 0; }
 
 __global__ void __launch_bounds__(WS_THREADS, 1) k_wgrad_small_tc(SmallArgs a)
 {
@@ -823,12 +869,13 @@ int plbm_nn_tc_conv(const void *x, const void *w, const float *bias, void *y, in
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
 }
 
-// The weight gradient runs on the tensor cores for Cin and Cout multiples of 32 up to 128 and the
+// The weight gradient runs on the TMA-fed tensor-core kernel for Cin a multiple of 32 up to 128,
+// Cout up to 128 (TMA gradient tiles for multiples of 32, written by two warps otherwise) and the
 // image tilings of the forward kernel.
 bool plbm_nn_tc_wgrad_supported(int H, int W, int Cin, int Cout)
 {
-    if (Cin % TC_KB != 0 || Cout % TC_KB != 0 || Cin > 128 || Cout > WG_M || Cin < TC_KB) return false;
-    return plbm_nn_tc_supported(H, W, Cin, Cout);
+    if (Cin % TC_KB != 0 || Cin < TC_KB || Cin > 128 || Cout < 1 || Cout > WG_M) return false;
+    return tiles_exactly(H, W);
 }
 
 // gw[co][tap][ci] += sum_p g[p][co] x[p + tap][ci] on the tensor cores (x, g NHWC BF16, gw FP32).
@@ -837,12 +884,22 @@ int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int 
     PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
     int *err = error_flag();
     if (!enc || !err) return PLBM_ERR_CUDA;
-    const int BW = W >= TC_BM ? TC_BM : W, BH = TC_BM / BW;
-    const int ntaps = 9 * Cin <= 512 ? 9 : 3;
-    const int b_bytes = (Cin / TC_KB) * WG_CHUNK;
-    const int stage = WG_A_BYTES + b_bytes;
-    const int stages = (200 * 1024) / stage < 4 ? (200 * 1024) / stage : 4;
-    const int smem = stages * stage + WG_SLACK + 1024 + 256;
+    WgArgs a{};
+    a.gw = gw; a.g = (const __nv_bfloat16 *)g;
+    a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout;
+    a.BW = W >= TC_BM ? TC_BM : W; a.BH = TC_BM / a.BW; a.tiles_x = W / a.BW; a.tiles_y = H / a.BH;
+    const int kbx = Cin / TC_KB;
+    a.ntaps = kbx == 1 ? 9 : 3;                    // the TMEM columns of a CTA stay <= 384
+    a.tg = a.ntaps * kbx <= 9 ? a.ntaps : 1;       // at most nine input tiles (72 KB) per stage
+    a.xchunks = a.tg * kbx;
+    a.gchunks = (Cout + TC_KB - 1) / TC_KB;
+    a.g_tma = Cout % TC_KB == 0;
+    a.stage_bytes = (a.xchunks + a.gchunks) * WG_CHUNK;
+    const int budget = 227 * 1024 - WG_SLACK - 1024 - 256;
+    a.stages = budget / a.stage_bytes < 4 ? budget / a.stage_bytes : 4;
+    if (a.stages < 2) return PLBM_ERR_ARGUMENT;
+    a.err = err;
+    const int smem = a.stages * a.stage_bytes + WG_SLACK + 1024 + 256;
     static int attr_bytes = 0;
     static std::mutex mu;
     {
@@ -854,12 +911,13 @@ int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int 
         }
     }
     CUtensorMap xmap, gmap;
+    memset(&gmap, 0, sizeof(gmap));
     const cuuint32_t es[4] = { 1, 1, 1, 1 };
-    for (int which = 0; which < 2; ++which) {
+    for (int which = 0; which < (a.g_tma ? 2 : 1); ++which) {
         const int C = which == 0 ? Cin : Cout;
         const cuuint64_t dims[4] = { (cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N };
         const cuuint64_t strides[3] = { (cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2 };
-        const cuuint32_t box[4] = { TC_KB, (cuuint32_t)BW, (cuuint32_t)BH, 1 };
+        const cuuint32_t box[4] = { TC_KB, (cuuint32_t)a.BW, (cuuint32_t)a.BH, 1 };
         if (enc(which == 0 ? &xmap : &gmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(which == 0 ? x : g),
                 dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
@@ -867,12 +925,11 @@ int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int 
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
-    const int groups = 9 / ntaps;
-    const int total = N * (W / BW) * (H / BH);
+    const int groups = 9 / a.ntaps;
+    a.total_tiles = N * a.tiles_x * a.tiles_y;
     const int chunks = (sms + groups - 1) / groups;
-    const int per = (total + chunks - 1) / chunks;
-    WgArgs a{ gw, N, H, W, Cin, Cout, BW, BH, W / BW, H / BH, ntaps, per, total, b_bytes, stage, stages, err };
-    k_wgrad_tc<<<dim3((total + per - 1) / per, groups), 128, smem, s>>>(xmap, gmap, a);
+    a.tiles_per_cta = (a.total_tiles + chunks - 1) / chunks;
+    k_wgrad_tc<<<dim3((a.total_tiles + a.tiles_per_cta - 1) / a.tiles_per_cta, groups), 128, smem, s>>>(xmap, gmap, a);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
 }
 
