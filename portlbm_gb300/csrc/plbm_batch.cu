@@ -83,7 +83,8 @@ __global__ void __launch_bounds__(256, PREC == F64_Q60 ? 3 : 6) k_batch(BatchArg
 }
 
 // 2-byte storage: the same queue, each warp updating 256-node row segments with the vectorised
-// row update of k_nptl_vec (blockDim.x == 32; a tile is 256 x (tile_h * tile_rows) nodes).  The
+// row update of k_nptl_vec_porous (bounce-back merged word-wise, no per-node branches away from the
+// domain edge; blockDim.x == 32; a tile is 256 x (tile_h * tile_rows) nodes).  The
 // queue loop is repeated rather than shared with k_batch through a tile-body lambda: that version
 // compiled k_batch<F32> with more spilled words and ran 1.8 % slower.
 template <int PREC>
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(256, 2) k_batch_vec(BatchArgs a)
         const int y0 = (local / txs) * a.tile_h * a.tile_rows + threadIdx.y;
         for (int r = 0; r < a.tile_rows; ++r) {
             const int yi = y0 + r * a.tile_h;
-            if (yi < sp.H) vec_row_segment<PREC>(sp, yi, xv, threadIdx.x);   // uniform over the warp
+            if (yi < sp.H) vec_row_segment_porous<PREC>(sp, yi, xv, threadIdx.x);   // uniform over the warp
         }
         if (tid == 0) s_tile = next;
         __syncthreads();

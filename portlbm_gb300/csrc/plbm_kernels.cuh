@@ -398,6 +398,145 @@ __device__ __forceinline__ void vec_row_segment(const StepParams &p, int y, int 
     }
 }
 
+// The row update for domains full of obstacles, without per-node branches away from the domain
+// edge.  Besides the nine shifted row loads, a lane loads its own row (y) of the six planes with a
+// vertical component when some lane of the warp has a solid source (the two horizontal planes were
+// loaded at row y already; their unshifted words are kept).  A population whose source is solid
+// bounces back, i.e. is the node's own value of the opposite direction: per direction the words
+// are merged under a mask built from the link words (bit d of each 16-bit half), and the
+// re-referencing shift is left out for those halves, as pull_one does.  Edge nodes keep the scalar
+// gather.  The same values as pull_one, i.e. as the other kernels.
+template <int PREC>
+__device__ __forceinline__ void vec_row_segment_porous(const StepParams &p, int y, int xv, int lane)
+{
+    static_assert(PREC == F16S || PREC == BF16S || PREC == F16C, "2-byte shifted storage only");
+    const bool vec_ok = xv < p.P;
+    const int x0 = vec_ok ? xv : p.P - VEC;
+    const unsigned short *S = static_cast<const unsigned short *>(p.lat0);
+    const size_t row0 = (size_t)y * p.P;
+    const bool inner_row = y > 0 && y < p.H - 1;
+
+    unsigned r[9][4];
+    const uint4 l4 = in_range(row0 + x0 + VEC - 1, p.N, p) ? *reinterpret_cast<const uint4 *>(p.links + row0 + x0)
+                                                         : make_uint4(0, 0, 0, 0);
+    const unsigned lw[4] = { l4.x, l4.y, l4.z, l4.w };
+    // bits 0-3 and 5-8 of both halves: a solid source (bit 4 marks fluid)
+    const bool bounce_here = ((lw[0] | lw[1] | lw[2] | lw[3]) & 0x01EF01EFu) != 0;
+    const bool bounce_warp = __any_sync(0xffffffffu, inner_row && bounce_here);
+    if (inner_row) {
+        unsigned o[6][4];   // own row of planes 0, 1, 2, 6, 7, 8
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {
+            const size_t at = (size_t)d * p.N + (size_t)(y - cyd(d)) * p.P + x0;
+            const uint4 v = in_range(at + VEC - 1, p.lat_elems, p) ? *reinterpret_cast<const uint4 *>(S + at)
+                                                                  : make_uint4(0, 0, 0, 0);
+            r[d][0] = v.x; r[d][1] = v.y; r[d][2] = v.z; r[d][3] = v.w;
+        }
+        if (bounce_warp) {
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+                const int e = i < 3 ? i : i + 3;
+                const size_t at = (size_t)e * p.N + row0 + x0;
+                const uint4 v = in_range(at + VEC - 1, p.lat_elems, p) ? *reinterpret_cast<const uint4 *>(S + at)
+                                                                      : make_uint4(0, 0, 0, 0);
+                o[i][0] = v.x; o[i][1] = v.y; o[i][2] = v.z; o[i][3] = v.w;
+            }
+        }
+        const unsigned own3[4] = { r[3][0], r[3][1], r[3][2], r[3][3] }, own5[4] = { r[5][0], r[5][1], r[5][2], r[5][3] };
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {
+            const unsigned short *row = S + (size_t)d * p.N + (size_t)(y - cyd(d)) * p.P;
+            if (cxd(d) == 1) {
+                unsigned prev = __shfl_up_sync(0xffffffffu, r[d][3] >> 16, 1);
+                if (lane == 0)
+                    prev = x0 >= 1 && in_range((size_t)(row - S) + x0 - 1, p.lat_elems, p) ? (unsigned)row[x0 - 1] : 0u;
+                r[d][3] = __byte_perm(r[d][2], r[d][3], 0x5432);
+                r[d][2] = __byte_perm(r[d][1], r[d][2], 0x5432);
+                r[d][1] = __byte_perm(r[d][0], r[d][1], 0x5432);
+                r[d][0] = __byte_perm(prev, r[d][0], 0x5410);
+            } else if (cxd(d) == -1) {
+                unsigned next = __shfl_down_sync(0xffffffffu, r[d][0] & 0xffffu, 1);
+                if (lane == 31)
+                    next = x0 + VEC < p.P && in_range((size_t)(row - S) + x0 + VEC, p.lat_elems, p) ? (unsigned)row[x0 + VEC]
+                                                                                                    : 0u;
+                r[d][0] = __byte_perm(r[d][0], r[d][1], 0x5432);
+                r[d][1] = __byte_perm(r[d][1], r[d][2], 0x5432);
+                r[d][2] = __byte_perm(r[d][2], r[d][3], 0x5432);
+                r[d][3] = __byte_perm(r[d][3], next, 0x5432);
+            }
+        }
+        if (bounce_warp) {
+#pragma unroll
+            for (int d = 0; d < 9; ++d) {
+                if (d == 4) continue;
+                const int e = 8 - d;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const unsigned own = e == 3 ? own3[k] : e == 5 ? own5[k] : o[e < 3 ? e : e - 3][k];
+                    const unsigned sel = ((lw[k] >> d) & 0x00010001u) * 0xFFFFu;
+                    r[d][k] = (r[d][k] & ~sel) | (own & sel);
+                }
+            }
+        }
+    } else {
+#pragma unroll
+        for (int d = 0; d < 9; ++d) r[d][0] = r[d][1] = r[d][2] = r[d][3] = 0u;
+    }
+    bool over = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float fa[9], fb[9];
+        const uint16_t la = (uint16_t)(lw[k] & 0xffffu), lb = (uint16_t)(lw[k] >> 16);
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {
+            // re-referenced unless bounced (-0.0f leaves a value exactly as loaded)
+            const float sh = cxd(d) != 0 ? p.shift_cx[d] : -0.0f;
+            const float2 v = vec_unpack<PREC>(r[d][k], -0.0f);
+            fa[d] = v.x + (((la >> d) & 1u) ? -0.0f : sh);
+            fb[d] = v.y + (((lb >> d) & 1u) ? -0.0f : sh);
+        }
+        const int xa = x0 + 2 * k, xb = xa + 1;
+        const bool live_a = vec_ok && xa < p.W && (la & LINK_FLUID), live_b = vec_ok && xb < p.W && (lb & LINK_FLUID);
+        if (live_a && (la & LINK_EDGE)) vec_edge_gather<PREC>(fa, xa, y, la, p);
+        if (live_b && (lb & LINK_EDGE)) vec_edge_gather<PREC>(fb, xb, y, lb, p);
+        if (live_a) {
+            const MomentsF m = collide<PREC>(fa, p);
+            emit_observables<PREC>(m, xa, y, p);
+        } else {
+#pragma unroll
+            for (int d = 0; d < 9; ++d) fa[d] = 0.0f;
+        }
+        if (live_b) {
+            const MomentsF m = collide<PREC>(fb, p);
+            emit_observables<PREC>(m, xb, y, p);
+        } else {
+#pragma unroll
+            for (int d = 0; d < 9; ++d) fb[d] = 0.0f;
+        }
+#pragma unroll
+        for (int d = 0; d < 9; ++d) r[d][k] = vec_pack<PREC>(fa[d], fb[d], over);
+    }
+    if constexpr (PREC == F16C)
+        if (over) atomicOr(p.status, 1);
+    if (!vec_ok) return;
+    unsigned short *D = static_cast<unsigned short *>(p.lat1);
+#pragma unroll
+    for (int d = 0; d < 9; ++d) {
+        const size_t at = (size_t)d * p.N + row0 + x0;
+        if (in_range(at + VEC - 1, p.lat_elems, p))
+            *reinterpret_cast<uint4 *>(D + at) = make_uint4(r[d][0], r[d][1], r[d][2], r[d][3]);
+    }
+}
+
+template <int PREC>
+__global__ void __launch_bounds__(32 * VEC_ROWS, 4) k_nptl_vec_porous(StepParams p)
+{
+    const int lane = threadIdx.x;                              // blockDim.x == 32: a warp is a row segment
+    const int y = blockIdx.y * VEC_ROWS + threadIdx.y;
+    if (y >= p.H) return;                                      // uniform over the warp
+    vec_row_segment_porous<PREC>(p, y, (blockIdx.x * 32 + lane) * VEC, lane);
+}
+
 template <int PREC>
 __global__ void __launch_bounds__(32 * VEC_ROWS, 4) k_nptl_vec(StepParams p)
 {

@@ -64,10 +64,10 @@ def test_q60_within_tolerance(plbm, oracle_mod, alg, lay):
 @pytest.mark.parametrize("precision", ["f16s", "bf16s", "f16c"])
 @pytest.mark.parametrize("w,h,porous", [(203, 61, True), (300, 40, True), (62, 30, False), (520, 20, True)])
 def test_vectorised_rows_match_scalar_kernel(plbm, precision, w, h, porous):
-    """nptl/stream runs the 2-byte forms 8 nodes per thread with warp shuffles (open gather); lptl,
-    the collision layout and the porous gather run the scalar kernels: same arithmetic,
-    bit-identical results (row lengths not a multiple of 8 or 256, porous obstacles, inlet,
-    outlet, walls)."""
+    """nptl/stream runs the 2-byte forms 8 nodes per thread with warp shuffles (open gather: solid
+    sources re-gathered node by node; porous gather: bounce-back merged word-wise); lptl and the
+    collision and bundle layouts run the scalar kernels: same arithmetic, bit-identical results
+    (row lengths not a multiple of 8 or 256, porous obstacles, inlet, outlet, walls)."""
     mask = plbm.porous_disks(w, h, 9, 0.7) if porous else None
     scen = "Hagen-Poiseuille" if porous else "circle"
     a = run_gpu(plbm, "nptl", "stream", scen, w, h, 300, precision=precision, mask=mask, gather="open")
