@@ -101,16 +101,23 @@ __device__ __forceinline__ void umma_commit(unsigned bar)
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-// Epilogue of one pixel: accumulator columns c0 .. c0 + 15 (FP32 bit patterns) plus the bias,
-// ReLU, rounded to BF16 and stored to out[c0 ..] for the channels below C; with C a multiple of 8,
-// as 16-byte stores of eight channels (a pixel row is 16-byte aligned then).
-__device__ __forceinline__ void store_row16(__nv_bfloat16 *out, int c0, int C, const unsigned v[16], const float *bias,
+// The bias of a CTA's output channels in shared memory (zero past Cout and without a bias), read by
+// every epilogue thread: npad <= 128 floats.
+__device__ __forceinline__ void stage_bias(float *sb, const float *bias, int Cout, int npad)
+{
+    for (int i = threadIdx.x; i < npad; i += blockDim.x) sb[i] = bias && i < Cout ? bias[i] : 0.f;
+}
+
+// Epilogue of one pixel: accumulator columns c0 .. c0 + 15 (FP32 bit patterns) plus the bias (sb,
+// shared memory), ReLU, rounded to BF16 and stored to out[c0 ..] for the channels below C; with C
+// a multiple of 8, as 16-byte stores of eight channels (a pixel row is 16-byte aligned then).
+__device__ __forceinline__ void store_row16(__nv_bfloat16 *out, int c0, int C, const unsigned v[16], const float *sb,
                                             int relu)
 {
     float f[16];
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-        f[j] = __uint_as_float(v[j]) + (bias && c0 + j < C ? bias[c0 + j] : 0.f);
+        f[j] = __uint_as_float(v[j]) + sb[c0 + j];
         if (relu) f[j] = fmaxf(f[j], 0.f);
     }
     if (C % 8 == 0) {
@@ -144,6 +151,7 @@ struct TcArgs {
 __global__ void __launch_bounds__(128, 4)
 k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap wmap, TcArgs a)
 {
+    __shared__ float s_bias[128];
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     // stages aligned to 1024 B (the swizzle pattern repeats every 512 B)
     unsigned char *smem = tc_smem_raw + ((1024 - (smem_u32(tc_smem_raw) & 1023)) & 1023);
@@ -165,6 +173,7 @@ k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUte
                      "r"(ncols) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
+    stage_bias(s_bias, a.bias, a.Cout, a.npad);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -230,7 +239,7 @@ k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUte
                      : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         if (!valid || py >= a.H || px >= a.W) continue;
-        store_row16(a.y + (((size_t)n * a.H + py) * a.W + px) * a.Cout, c0, a.Cout, v, a.bias, a.relu);
+        store_row16(a.y + (((size_t)n * a.H + py) * a.W + px) * a.Cout, c0, a.Cout, v, s_bias, a.relu);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -551,6 +560,7 @@ struct SmallArgs {
 // one thread issues kchunks * 2 MMAs (K = 16 each) into a TMEM accumulator of npad columns.
 __global__ void __launch_bounds__(SM_BUILD, 8) k_conv_small_tc(SmallArgs a)
 {
+    __shared__ float s_bias[128];
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     unsigned char *smem = tc_smem_raw + ((1024 - (smem_u32(tc_smem_raw) & 1023)) & 1023);
     unsigned char *As = smem, *Bs = smem + a.kchunks * WG_CHUNK;
@@ -568,6 +578,7 @@ __global__ void __launch_bounds__(SM_BUILD, 8) k_conv_small_tc(SmallArgs a)
                      "r"(ncols) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
+    stage_bias(s_bias, a.bias, a.Cout, a.npad);
     const int per_img = a.tiles_x * a.tiles_y;
     const int n = blockIdx.x / per_img, t2 = blockIdx.x % per_img;
     const int y0 = (t2 / a.tiles_x) * a.BH, x0 = (t2 % a.tiles_x) * a.BW;
@@ -622,7 +633,7 @@ __global__ void __launch_bounds__(SM_BUILD, 8) k_conv_small_tc(SmallArgs a)
                      : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         if (!valid || py >= a.H || px >= a.W) continue;
-        store_row16(a.y + (((size_t)n * a.H + py) * a.W + px) * a.Cout, c0, a.Cout, v, a.bias, a.relu);
+        store_row16(a.y + (((size_t)n * a.H + py) * a.W + px) * a.Cout, c0, a.Cout, v, s_bias, a.relu);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -649,7 +660,7 @@ __global__ void __launch_bounds__(SM_BUILD, 8) k_conv_small_tc(SmallArgs a)
 // w of an M tile, lane = (tap, ci) column) and add them to dW[co][(tap, ci)] with FP32 atomics.
 constexpr int WS_THREADS = 256, WS_BATCH = 10;
 
-__global__ void __launch_bounds__(WS_THREADS, 1) k_wgrad_small_tc(SmallArgs a)
+__global__ void __launch_bounds__(WS_THREADS, 2) k_wgrad_small_tc(SmallArgs a)
 {
     extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
     unsigned char *smem = tc_smem_raw + ((1024 - (smem_u32(tc_smem_raw) & 1023)) & 1023);
@@ -771,6 +782,188 @@ __global__ void __launch_bounds__(WS_THREADS, 1) k_wgrad_small_tc(SmallArgs a)
     }
 }
 
+// ---- forward convolution with halo rows (W a multiple of 128) ---------------------------------
+// A tile is 128 pixels of one image row.  Instead of nine shifted input tiles per 32-channel block,
+// the three input rows y0 - 1, y0, y0 + 1 are loaded once as halo rows of 136 pixels (x0 - 1 ..
+// x0 + 134, TMA zero fill outside the image), and tap (dy, dx) reads the 128 rows of halo row dy + 1
+// that start at pixel dx + 1, i.e. a descriptor start address 64 * (dx + 1) bytes into the row
+// buffer: 26 KB per block instead of 72 KB.  The tensor cores apply the 64-byte swizzle to the
+// address bits, as the TMA wrote the rows, so such a start needs no base offset in the descriptor
+// (measured: with the base offset set from the start address the results are wrong).  The weights of the whole layer stay in shared memory
+// (loaded once per CTA) and CTAs are persistent (one per SM).  A CTA's tiles alternate between two
+// pipelines, each with its own ring of stages, its own MMA-issuing thread (warps 1 and 6) and two
+// TMEM accumulators: one thread issues a tcgen05.mma about every 100 cycles (measured), so a
+// single issuer leaves the tensor pipe idle three quarters of the time at N <= 128.  Warp 0 loads
+// for both, warps 2..5 drain the accumulators in tile order (bias, ReLU, BF16 stores) while the
+// next tiles accumulate.
+constexpr int HALO_ROW = 136;                         // pixels of a halo row (a multiple of 8)
+constexpr int HALO_ROW_BYTES = 9216;                  // HALO_ROW * 64 B rounded up to 1024 B
+constexpr int HALO_STAGE = 3 * HALO_ROW_BYTES;        // three rows of one 32-channel block
+constexpr int HALO_MAX_STAGES = 3;            // per pipeline
+
+struct HaloArgs {
+    __nv_bfloat16 *y;
+    const float *bias;      // may be null
+    int N, H, W, Cin, Cout, npad, relu;
+    int tiles_x, tiles;     // 128-pixel tiles per image row, in all
+    int kblocks, stages, w_bytes;
+    int *err;
+};
+
+
+__global__ void __launch_bounds__(224, 1)
+k_conv_halo_tc(const __grid_constant__ CUtensorMap hmap, const __grid_constant__ CUtensorMap wmap, HaloArgs a)
+{
+    __shared__ float s_bias[128];
+    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+    unsigned char *smem = tc_smem_raw + ((1024 - (smem_u32(tc_smem_raw) & 1023)) & 1023);
+    const int S = a.stages, NS = 2 * S;       // stages per pipeline, in all
+    unsigned char *wts = smem, *rows = smem + a.w_bytes;
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(rows + NS * HALO_STAGE);
+    unsigned long long *full = bars, *empty = bars + NS, *tfull = bars + 2 * NS, *tempty = tfull + 4,
+                       *wfull = tempty + 4, *done = wfull + 1;
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(done + 2);
+    int *counts = reinterpret_cast<int *>(tmem_slot + 1);   // [p] issued, [2 + p] consumed, [4] failed
+    volatile int *failed = &counts[4];
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned ncols = 4 * a.npad <= 64 ? 64u : 4 * a.npad <= 128 ? 128u : 4 * a.npad <= 256 ? 256u : 512u;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NS; ++s) { mbar_init(smem_u32(&full[s]), 1); mbar_init(smem_u32(&empty[s]), 1); }
+        for (int b = 0; b < 4; ++b) { mbar_init(smem_u32(&tfull[b]), 1); mbar_init(smem_u32(&tempty[b]), 4); }
+        mbar_init(smem_u32(wfull), 1);
+        mbar_init(smem_u32(&done[0]), 1);
+        mbar_init(smem_u32(&done[1]), 1);
+        for (int k = 0; k < 5; ++k) counts[k] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(ncols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    stage_bias(s_bias, a.bias, a.Cout, a.npad);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = *tmem_slot;
+    const int per_img = a.tiles_x * a.H;
+    const unsigned wchunk = (unsigned)a.npad * 64u;
+    // the CTA's tiles t_i = blockIdx.x + i * gridDim.x alternate between the pipelines: p = i & 1
+    const int ntiles = a.tiles > (int)blockIdx.x ? (a.tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+
+    if (warp == 0 && lane == 0) {              // producer: the weights once, then the halo rows in tile order
+        mbar_expect_tx(smem_u32(wfull), (unsigned)(9 * a.kblocks) * wchunk);
+        for (int kb = 0; kb < a.kblocks; ++kb)
+            for (int tap = 0; tap < 9; ++tap)
+                tma_load_3d(smem_u32(wts + (kb * 9 + tap) * wchunk), &wmap, kb * TC_KB, tap, 0, smem_u32(wfull));
+        for (int i = 0; i < ntiles && !*failed; ++i) {
+            const int t = blockIdx.x + i * gridDim.x, p = i & 1, ip = i >> 1;
+            const int n = t / per_img, r = t % per_img, y0 = r / a.tiles_x, x0 = (r % a.tiles_x) * TC_BM;
+            for (int kb = 0; kb < a.kblocks; ++kb) {
+                const int itp = ip * a.kblocks + kb, s = p * S + itp % S;
+                if (itp >= S && !mbar_wait(smem_u32(&empty[s]), (unsigned)((itp / S - 1) & 1))) {
+                    *failed = 1;
+                    break;
+                }
+                const unsigned bar = smem_u32(&full[s]);
+                mbar_expect_tx(bar, 3u * HALO_ROW * 64u);
+                for (int dy = 0; dy < 3; ++dy)
+                    tma_load_4d(smem_u32(rows + s * HALO_STAGE + dy * HALO_ROW_BYTES), &hmap, kb * TC_KB, x0 - 1,
+                                y0 + dy - 1, n, bar);
+                counts[p] = itp + 1;
+            }
+        }
+    } else if ((warp == 1 || warp == 6) && lane == 0) {   // MMA issuers, one per pipeline
+        const int p = warp == 1 ? 0 : 1;
+        const unsigned idesc = instr_desc(a.npad);
+        if (!mbar_wait(smem_u32(wfull), 0)) *failed = 1;
+        const uint64_t bstep = wchunk >> 4;
+        for (int ip = 0; 2 * ip + p < ntiles && !*failed; ++ip) {
+            const int b = ip & 1, acc = p * 2 + b;
+            if (ip >= 2 && !mbar_wait(smem_u32(&tempty[acc]), (unsigned)(((ip >> 1) - 1) & 1))) {
+                *failed = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const unsigned d = tmem + (unsigned)(acc * a.npad);
+            for (int kb = 0; kb < a.kblocks; ++kb) {
+                const int itp = ip * a.kblocks + kb, s = p * S + itp % S;
+                if (!mbar_wait(smem_u32(&full[s]), (unsigned)((itp / S) & 1))) {
+                    *failed = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                // descriptors of the stage's first row and the block's first tap; the others differ only
+                // in the start-address field (bytes / 16, no carry below 256 KB): one add per operand
+                const uint64_t ad0 = smem_desc_sw64(smem_u32(rows + s * HALO_STAGE));
+                const uint64_t bd0 = smem_desc_sw64(smem_u32(wts + kb * 9 * wchunk));
+#pragma unroll
+                for (int tap = 0; tap < 9; ++tap)
+#pragma unroll
+                    for (int k = 0; k < TC_KB / 16; ++k)
+                        umma(d, ad0 + (uint64_t)(((tap / 3) * HALO_ROW_BYTES + (tap % 3) * 64 + 32 * k) >> 4),
+                             bd0 + (uint64_t)tap * bstep + (uint64_t)(2 * k), idesc, kb > 0 || tap > 0 || k > 0);
+                umma_commit(smem_u32(&empty[s]));
+                counts[2 + p] = itp + 1;
+            }
+            umma_commit(smem_u32(&tfull[acc]));
+        }
+        umma_commit(smem_u32(&done[p]));
+    } else if (warp >= 2 && warp <= 5) {       // epilogue: TMEM lanes 32 * (warp % 4) .., tiles in order
+        const int sub = warp & 3, row = sub * 32 + lane;
+        for (int i = 0; i < ntiles; ++i) {
+            const int t = blockIdx.x + i * gridDim.x, p = i & 1, ip = i >> 1, acc = p * 2 + (ip & 1);
+            bool ok = true;
+            if (lane == 0) ok = mbar_wait(smem_u32(&tfull[acc]), (unsigned)((ip >> 1) & 1));
+            if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) {
+                if (lane == 0) *failed = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int n = t / per_img, r = t % per_img, y0 = r / a.tiles_x, px = (r % a.tiles_x) * TC_BM + row;
+            __nv_bfloat16 *out = a.y + (((size_t)n * a.H + y0) * a.W + px) * a.Cout;
+            for (int c0 = 0; c0 < a.npad; c0 += 32) {   // two 16-column loads per wait (npad: a multiple of 16)
+                unsigned v[2][16];
+                const unsigned taddr = tmem + ((unsigned)(sub * 32) << 16) + (unsigned)(acc * a.npad + c0);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (c0 + 16 * h >= a.npad) break;
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                                 : "=r"(v[h][0]), "=r"(v[h][1]), "=r"(v[h][2]), "=r"(v[h][3]), "=r"(v[h][4]), "=r"(v[h][5]),
+                                   "=r"(v[h][6]), "=r"(v[h][7]), "=r"(v[h][8]), "=r"(v[h][9]), "=r"(v[h][10]), "=r"(v[h][11]),
+                                   "=r"(v[h][12]), "=r"(v[h][13]), "=r"(v[h][14]), "=r"(v[h][15])
+                                 : "r"(taddr + 16u * h));
+                }
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                store_row16(out, c0, a.Cout, v[0], s_bias, a.relu);
+                if (c0 + 16 < a.npad) store_row16(out, c0 + 16, a.Cout, v[1], s_bias, a.relu);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[acc])) : "memory");
+        }
+    }
+    if (threadIdx.x == 0) {   // every issued MMA has completed (each issuer commits its own)
+        if (!mbar_wait(smem_u32(&done[0]), 0) || !mbar_wait(smem_u32(&done[1]), 0)) *failed = 1;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && *failed) {
+        atomicExch(a.err, 1);
+        // after a failed wait: the weights and the halo rows still in flight, each bounded
+        mbar_wait(smem_u32(wfull), 0);
+        for (int p = 0; p < 2; ++p)
+            for (int itp = counts[2 + p]; itp < counts[p]; ++itp)
+                mbar_wait(smem_u32(&full[p * S + itp % S]), (unsigned)((itp / S) & 1));
+    }
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+}
+
 // Wt[ci][tap][co] = W[co][8 - tap][ci]: the weights of the input-gradient convolution.
 __global__ void k_flip_weights(const __nv_bfloat16 *w, __nv_bfloat16 *wt, int Cin, int Cout)
 {
@@ -861,6 +1054,40 @@ int plbm_nn_tc_conv(const void *x, const void *w, const float *bias, void *y, in
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return PLBM_ERR_ARGUMENT;
     }
+    // rows of 128 pixels: the halo-row kernel, when the layer's weights and two stages fit
+    const int kblocks = Cin / TC_KB;
+    const int w_bytes = 9 * kblocks * npad * 64;
+    const int halo_budget = 227 * 1024 - 1024 - 512 - 1024;   // less alignment, barriers, the static bias array
+    const int hfit = (halo_budget - w_bytes) / (2 * HALO_STAGE);   // stages per pipeline (two pipelines)
+    const int hstages = hfit < HALO_MAX_STAGES ? hfit : HALO_MAX_STAGES;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    // each persistent CTA loads the whole layer's weights first: worth it from four tiles per SM on
+    if (W % TC_BM == 0 && hstages >= 1 && N * H * (W / TC_BM) >= 4 * sms) {
+        CUtensorMap hmap;
+        const cuuint64_t dims[4] = { (cuuint64_t)Cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N };
+        const cuuint64_t strides[3] = { (cuuint64_t)Cin * 2, (cuuint64_t)W * Cin * 2, (cuuint64_t)H * W * Cin * 2 };
+        const cuuint32_t box[4] = { TC_KB, HALO_ROW, 1, 1 };
+        const cuuint32_t es[4] = { 1, 1, 1, 1 };
+        if (enc(&hmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(x), dims, strides, box, es,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return PLBM_ERR_ARGUMENT;
+        const int smem = w_bytes + 2 * hstages * HALO_STAGE + 1024 + 512;
+        static int halo_attr = 0;
+        {
+            std::lock_guard<std::mutex> g(mu);
+            if (smem > halo_attr) {
+                if (cudaFuncSetAttribute(k_conv_halo_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+                    return PLBM_ERR_CUDA;
+                halo_attr = smem;
+            }
+        }
+        HaloArgs h{ (__nv_bfloat16 *)y, bias, N, H, W, Cin, Cout, npad, relu, W / TC_BM, N * H * (W / TC_BM),
+                    kblocks, hstages, w_bytes, err };
+        k_conv_halo_tc<<<h.tiles < sms ? h.tiles : sms, 224, smem, s>>>(hmap, wmap, h);
+        return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+    }
     // stages sized by the padded output channels, so narrow layers fit more CTAs per SM
     const int stage = TC_A_BYTES + (npad * TC_KB * 2 + 1023) / 1024 * 1024;
     TcArgs a{ (__nv_bfloat16 *)y, bias, N, H, W, Cin, Cout, npad, relu, BW, BH, W / BW, H / BH, stage, err };
@@ -895,6 +1122,8 @@ int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int 
     a.gchunks = (Cout + TC_KB - 1) / TC_KB;
     a.g_tma = Cout % TC_KB == 0;
     a.stage_bytes = (a.xchunks + a.gchunks) * WG_CHUNK;
+    // one CTA per SM with 2-4 stages (two CTAs of one stage each measured slower: each then waits
+    // out its own load latency)
     const int budget = 227 * 1024 - WG_SLACK - 1024 - 256;
     a.stages = budget / a.stage_bytes < 4 ? budget / a.stage_bytes : 4;
     if (a.stages < 2) return PLBM_ERR_ARGUMENT;
@@ -927,7 +1156,9 @@ int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     const int groups = 9 / a.ntaps;
     a.total_tiles = N * a.tiles_x * a.tiles_y;
-    const int chunks = (sms + groups - 1) / groups;
+    // one CTA per SM (the stages fill its shared memory): groups x chunks must not exceed the SMs,
+    // or the CTAs past them run as a second wave
+    const int chunks = sms / groups > 0 ? sms / groups : 1;
     a.tiles_per_cta = (a.total_tiles + chunks - 1) / chunks;
     k_wgrad_tc<<<dim3((a.total_tiles + a.tiles_per_cta - 1) / a.tiles_per_cta, groups), 128, smem, s>>>(xmap, gmap, a);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
@@ -991,7 +1222,9 @@ int plbm_nn_tc_small_wgrad(const void *x, const void *g, float *gw, int N, int H
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     a.total_tiles = N * a.tiles_x * a.tiles_y;
-    a.tiles_per_cta = (a.total_tiles + sms - 1) / sms;
+    // two CTAs per SM (two MMA issuers, one building while the other's MMAs run) where they fit
+    const int per_sm = 2 * smem <= 227 * 1024 ? 2 : 1;
+    a.tiles_per_cta = (a.total_tiles + per_sm * sms - 1) / (per_sm * sms);
     k_wgrad_small_tc<<<(a.total_tiles + a.tiles_per_cta - 1) / a.tiles_per_cta, WS_THREADS, smem, s>>>(a);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
 }

@@ -70,10 +70,13 @@ def test_conv_forward_and_gradients(plbm, n, h, w, cin, cout):
 
 
 @pytest.mark.parametrize("n,h,w,cin,cout", [(2, 8, 256, 32, 32), (1, 16, 128, 128, 96), (3, 4, 64, 64, 48),
-                                           (2, 32, 16, 32, 16), (1, 16, 32, 96, 128)])
+                                           (2, 32, 16, 32, 16), (1, 16, 32, 96, 128), (1, 3, 256, 64, 64),
+                                           (2, 2, 128, 96, 64), (1, 5, 384, 64, 32), (1, 2, 128, 32, 3)])
 def test_tensor_core_convolution(plbm, n, h, w, cin, cout):
     """The tcgen05 path (TMA-staged implicit GEMM, TMEM accumulator) against the CPU oracle, for the
-    forward pass and, with the channel counts exchanged, the input gradient."""
+    forward pass and, with the channel counts exchanged, the input gradient.  Rows of a multiple of
+    128 pixels whose weights fit in shared memory run the persistent halo-row kernel (three halo
+    rows per 32-channel block, tap operands at 0, 64 and 128 bytes into a row buffer)."""
     import torch
     lib = _lib(plbm)
     lib.plbm_nn_conv_on_tensor_cores.argtypes = [ctypes.c_int] * 4
