@@ -605,10 +605,29 @@ __global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::b
     const int lx = threadIdx.x, ly = threadIdx.y;
     CT<PREC> f[9];
     if (fluid) {
-        if (lk == LINK_FLUID && lx > 0 && lx < TW - 1 && ly > 0 && ly < TH - 1) {
-            // inside the tile, away from the domain edge, all sources fluid
+        if (lk == LINK_FLUID) {
+            // away from the domain edge, all sources fluid: each source is in the tile, in the
+            // left/right neighbour's column snapshot or in the upper/lower neighbour's row snapshot.
+            // The choice is a select per direction, so the lanes on a tile edge (two in every warp
+            // of a 32-wide tile) run the same instructions as the others instead of a second,
+            // divergent pass.  A tile-edge lane here is never on the domain edge, so the
+            // neighbouring tile it selects exists; the index of an unselected branch is unused.
 #pragma unroll
-            for (int d = 0; d < 9; ++d) f[d] = ld<PREC>(p.lat0, lidx<L>(n, d, p.N) + pull_delta<L>(d, p), d, p);
+            for (int d = 0; d < 9; ++d) {
+                const int cx = cxd(d), cy = cyd(d);
+                const bool col = (cx == 1 && lx == 0) || (cx == -1 && lx == TW - 1);
+                const bool row = !col && ((cy == 1 && ly == 0) || (cy == -1 && ly == TH - 1));
+                unsigned long long i = lidx<L>(n, d, p.N) + pull_delta<L>(d, p);
+                if (cx != 0) {
+                    const unsigned long long ic = halo_col(p, cx == 1 ? tcx - 1 : tcx, yi - cy, cx == 1 ? d / 3 : 3 + d / 3);
+                    i = col ? ic : i;
+                }
+                if (cy != 0) {
+                    const unsigned long long ir = halo_row(p, cy == 1 ? tcy - 1 : tcy, xi - cx, cy == 1 ? d - 6 : 3 + d);
+                    i = row ? ir : i;
+                }
+                f[d] = ld<PREC>(col || row ? p.halo_in : p.lat0, i, d, p);
+            }
         } else {
 #pragma unroll
             for (int d = 0; d < 9; ++d) {
