@@ -319,6 +319,27 @@ def precision_study(plbm, w=1024, h=256, seed=12345, porosity=0.7, target=1e-6, 
             rec, out = run_to_steady(prec, mask, w, h)
             l2, dm = errs(out, ref, fluid)
             study[prec] = dict(rec, rel_l2_j_vs_f64=l2, mass_rel_diff_vs_f64=dm)
+        # the 16-bit forms finished in FP32: stepped in 16 bits until a 1000-step chunk no longer
+        # lowers the residual (the form's rounding floor), re-encoded in FP32 (plbm_set_precision),
+        # on to the target; then on towards ref_target for the comparison
+        rec, _ = run_to_steady("f64_q60", mask, w, h)
+        study["f64_q60_to_target"] = {"steps": rec["steps_to_target"], "seconds": rec["seconds_to_target"]}
+        for prec in [f for f in forms if f in ("f16s", "f16c", "bf16s")]:
+            props = plbm.Properties("nptl", "stream", False, 1024, 10 ** 9, 10 ** 9, "Hagen-Poiseuille", h, w, 0.0,
+                                    0.0, 1.01, 0.0, 0.0, 1.0, 0.6)
+            hd = plbm.create_handler(props, precision=prec, mask=mask)
+            t0 = time.perf_counter()
+            n1, r1, switched = hd.run_to_residual_escalating(target, 100, max_steps)
+            dt = time.perf_counter() - t0
+            n2, r2 = hd.run_to_residual(ref_target, 100, max_steps - n1) if n1 < max_steps else (0, r1)
+            out = (hd.get_densities(), hd.get_x_velocities(), hd.get_y_velocities())
+            hd.close()
+            l2, dm = errs(out, ref, fluid)
+            reached = r1 < target
+            study[prec + "_then_f32"] = {"steps_to_target": n1 if reached else None,
+                                         "seconds_to_target": round(dt, 3) if reached else None,
+                                         "switched_at_step": switched, "steps": n1 + n2, "residual": r2,
+                                         "rel_l2_j_vs_f64": l2, "mass_rel_diff_vs_f64": dm}
     bw, bh = big
     bmask = plbm.porous_disks(bw, bh, seed, porosity)
     bfl = bmask.reshape(-1) == 0

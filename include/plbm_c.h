@@ -248,6 +248,12 @@ const char *plbm_noalloc_last_error(void);
  * Results on the host are those of the last step. */
 int plbm_run_to_residual(plbm_handler *h, double target, unsigned K, unsigned max_steps, unsigned *steps,
                          double *residual);
+/* Re-encodes the state of a handler that is not stepping into another shifted storage form
+ * (PLBM_F32, PLBM_F16S, PLBM_BF16S, PLBM_F16C) and continues in it: every shifted form stores the
+ * deviation from the same reference state, so each lattice (and halo) value is decoded, rescaled
+ * exactly and rounded once.  Used to finish a 16-bit run in FP32 once the 16-bit form has reached
+ * its rounding floor.  PLBM_ERR_NUMERIC, handler unchanged, when the state does not fit F16C. */
+int plbm_set_precision(plbm_handler *h, int precision);
 /* Porous channel geometry: solid walls on the first and last inner rows plus non-overlapping disks
  * (radius uniform in [rmin, rmax]) placed at seeded random positions until the fluid fraction of
  * the interior drops to `porosity`.  out: W*H int8 (0 fluid, 1 solid).  Returns the disk count

@@ -129,6 +129,7 @@ _SIGS = {
     "plbm_benchmark_work_group_sizes": (ctypes.c_int, [ctypes.c_uint, ctypes.POINTER(ctypes.c_uint), ctypes.c_uint,
                                                        ctypes.POINTER(ctypes.c_uint)]),
     "plbm_set_equilibrium": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "plbm_set_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "plbm_run_to_residual": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_uint, ctypes.c_uint,
                                             ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(ctypes.c_double)]),
     "plbm_porous_disks": (ctypes.c_int, [ctypes.c_uint, ctypes.c_uint, ctypes.c_uint64, ctypes.c_double,
@@ -419,6 +420,29 @@ class AlgorithmHandler:
         steps, r = ctypes.c_uint(), ctypes.c_double()
         self._call("plbm_run_to_residual", float(target), int(k), int(max_steps), ctypes.byref(steps), ctypes.byref(r))
         return steps.value, r.value
+
+    def set_precision(self, precision: str) -> None:
+        """Re-encodes the state in another shifted storage form ("f32", "f16s", "bf16s", "f16c") and
+        continues in it (plbm_set_precision)."""
+        self._call("plbm_set_precision", PRECISIONS[precision])
+
+    def run_to_residual_escalating(self, target: float = 1e-6, k: int = 100, max_steps: int = 1_000_000,
+                                   chunk: int = 1000, stall: float = 0.95, then: str = "f32") -> tuple:
+        """Steps a 16-bit form towards the residual target; when a chunk of `chunk` steps no longer
+        lowers the residual below `stall` times its previous value (the form's rounding floor), the
+        state is re-encoded in `then` (FP32) and the run continues there.  Returns (steps, residual,
+        steps before the switch, or None when the target was met without one)."""
+        total, prev, switched = 0, None, None
+        while total < max_steps:
+            n, r = self.run_to_residual(target, k, min(chunk, max_steps - total))
+            total += n
+            if r < target:
+                return total, r, switched
+            if switched is None and prev is not None and r > stall * prev:
+                self.set_precision(then)
+                switched = total
+            prev = r
+        return total, prev, switched
 
     def bytes_per_node(self) -> float:
         v = ctypes.c_double()

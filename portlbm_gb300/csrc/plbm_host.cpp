@@ -1269,6 +1269,74 @@ int plbm_run_steps(plbm_handler *h, unsigned n, double *ms_per_step)
     });
 }
 
+// Re-encodes the state of a handler that is not stepping into another shifted storage form and
+// continues in it: the lattices (and npol's halo snapshots) hold the deviation from the same
+// reference state in every shifted form, so each value is decoded, rescaled by a power of two and
+// rounded once into the new form; the form's FP32 constants are rebuilt and the captured CUDA graphs
+// dropped.  A state that does not fit the new form (F16C) leaves the handler unchanged.
+int plbm_set_precision(plbm_handler *h, int precision)
+{
+    return guarded(h, [&] {
+        auto shifted = [](int p) { return p == PLBM_F32 || p == PLBM_F16S || p == PLBM_BF16S || p == PLBM_F16C; };
+        if (h->worker.joinable()) fail(PLBM_ERR_ARGUMENT, "plbm_set_precision while the step loop runs");
+        if (!shifted(h->prec) || !shifted(precision))
+            fail(PLBM_ERR_ARGUMENT, "plbm_set_precision converts between the shifted forms PLBM_F32, PLBM_F16S, "
+                                    "PLBM_BF16S and PLBM_F16C");
+        if (precision == h->prec) return;
+        cuda_check(cudaSetDevice(h->opt.device), "cudaSetDevice");
+        cuda_check(cudaStreamSynchronize(h->stream), "pending work");
+        plbm::StepParams b = h->base;
+        plbm::fill_float_constants(b, true, h->two_lattice(), h->props.irho, h->props.orho,
+                                   precision == PLBM_F16S ? (double)plbm::F16_SCALE : 1.0);
+        if (precision == PLBM_F16C) {
+            double worst = 0;
+            for (int d = 0; d < 9; ++d)
+                worst = std::max({ worst, std::fabs((double)b.weightf[d]), std::fabs((double)b.feq_inf[d]),
+                                   std::fabs((double)b.feq_outf[d]),
+                                   std::fabs((double)b.weightf[d] + (double)b.shift_wg[d] * (h->W - 1)) });
+            if (!(worst < 0.5))
+                fail(PLBM_ERR_NUMERIC, "f16c stores deviations |f - w rho0| < 0.5; these boundary densities exceed it");
+        }
+        const size_t eb = storage_bytes(precision);
+        const int nl = h->two_lattice() ? 2 : 1;
+        void *nlat[2] = { nullptr, nullptr }, *nhalo[2] = { nullptr, nullptr };
+        const size_t hn = h->alg == 2 ? std::max<size_t>(b.halo_elems, 1) : 0;
+        auto release_new = [&] {
+            for (auto &q : nlat) { if (q) cudaFree(q); q = nullptr; }
+            for (auto &q : nhalo) { if (q) cudaFree(q); q = nullptr; }
+        };
+        try {
+            cuda_check(cudaMemsetAsync(h->status_d, 0, sizeof(int), h->stream), "memset status");
+            for (int i = 0; i < nl; ++i) {
+                cuda_check(cudaMalloc(&nlat[i], 9ull * h->N * eb), "cudaMalloc lattice");
+                cuda_check(plbm::launch_convert_shifted(h->lat[i], h->prec, nlat[i], precision, 9ull * h->N, h->status_d,
+                                                        h->stream), "lattice conversion");
+            }
+            for (int i = 0; i < 2 && hn; ++i) {
+                cuda_check(cudaMalloc(&nhalo[i], hn * eb), "cudaMalloc halo");
+                cuda_check(plbm::launch_convert_shifted(h->halo[i], h->prec, nhalo[i], precision, b.halo_elems,
+                                                        h->status_d, h->stream), "halo conversion");
+            }
+            int st = 0;
+            cuda_check(cudaMemcpyAsync(&st, h->status_d, sizeof(int), cudaMemcpyDeviceToHost, h->stream), "status");
+            cuda_check(cudaStreamSynchronize(h->stream), "conversion");
+            if (st) fail(PLBM_ERR_NUMERIC, "the state does not fit the new storage form (f16c: |f - w rho0| < 0.5)");
+        } catch (...) {
+            release_new();
+            throw;
+        }
+        for (int i = 0; i < nl; ++i) { cudaFree(h->lat[i]); h->lat[i] = nlat[i]; nlat[i] = nullptr; }
+        for (int i = 0; i < 2 && hn; ++i) { cudaFree(h->halo[i]); h->halo[i] = nhalo[i]; nhalo[i] = nullptr; }
+        h->base = b;
+        h->prec = precision;
+        if (h->gexec) cudaGraphExecDestroy(h->gexec);
+        h->gexec = nullptr;
+        h->graph_steps = 0;
+        for (auto &f : h->frame_gexec) { if (f) cudaGraphExecDestroy(f); f = nullptr; }
+        h->frame_graph_len = 0;
+    });
+}
+
 int plbm_run_to_residual(plbm_handler *h, double target, unsigned K, unsigned max_steps, unsigned *steps,
                          double *residual)
 {

@@ -28,6 +28,9 @@ cudaError_t launch_fill_lattice(void *lat, int prec, int lay, unsigned long long
 cudaError_t launch_fill_shifted(void *lat, int prec, int lay, int P, unsigned long long N, const double w[9], double a,
                                 double g, cudaStream_t s);
 cudaError_t launch_fill_halo(void *halo, int prec, int W, int H, int ncb, int nrb, const double w[9], cudaStream_t s);
+// n entries of a shifted-form lattice (F32, F16S, BF16S, F16C) re-encoded in another shifted form
+cudaError_t launch_convert_shifted(const void *src, int src_prec, void *dst, int dst_prec, unsigned long long n,
+                                   int *status, cudaStream_t s);
 cudaError_t launch_fill_results(double *rho, double *jx, double *jy, double *ja, unsigned long long n, cudaStream_t s);
 // FP64 sums over fluid nodes of the result arrays: out3 = {sum rho, sum jx, sum jy}.
 cudaError_t launch_reduce_results(const double *rho, const double *jx, const double *jy, const int8_t *flags,

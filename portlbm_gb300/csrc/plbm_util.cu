@@ -159,6 +159,64 @@ cudaError_t launch_fill_shifted(void *lat, int prec, int lay, int P, unsigned lo
     return cudaGetLastError();
 }
 
+// A lattice or halo snapshot of one shifted storage form re-encoded in another.  Both hold the
+// deviation df = f - w_d rho0(x') from the same reference state (the FP16 form scaled by F16_SCALE,
+// a power of two): the value is decoded to FP32, rescaled exactly and rounded once into the new
+// form; a value beyond the F16C range sets bit 0 of *status.
+template <int SRC, int DST>
+__global__ void k_convert_shifted(const void *src, void *dst, unsigned long long n, int *status)
+{
+    using TS = typename Store<SRC>::T;
+    using TD = typename Store<DST>::T;
+    bool over = false;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const TS s = static_cast<const TS *>(src)[i];
+        float v;
+        if constexpr (SRC == F16S) v = __half2float(s) * (1.0f / F16_SCALE);
+        else if constexpr (SRC == BF16S) v = __bfloat162float(s);
+        else if constexpr (SRC == F16C) v = f16c_value(s);
+        else v = s;
+        TD *d = static_cast<TD *>(dst);
+        if constexpr (DST == F16S) d[i] = __float2half_rn(v * F16_SCALE);
+        else if constexpr (DST == BF16S) d[i] = __float2bfloat16_rn(v);
+        else if constexpr (DST == F16C) {
+            bool o;
+            d[i] = (unsigned short)f16c_bits(v, o);
+            over |= o;
+        } else d[i] = v;
+    }
+    if (over) atomicOr(status, 1);
+}
+
+template <int SRC>
+static cudaError_t convert_from(const void *src, int dst_prec, void *dst, unsigned long long n, int *status,
+                                cudaStream_t s)
+{
+    const int grid = 152 * 8, block = 256;
+    switch (dst_prec) {
+    case F32: k_convert_shifted<SRC, F32><<<grid, block, 0, s>>>(src, dst, n, status); break;
+    case F16S: k_convert_shifted<SRC, F16S><<<grid, block, 0, s>>>(src, dst, n, status); break;
+    case BF16S: k_convert_shifted<SRC, BF16S><<<grid, block, 0, s>>>(src, dst, n, status); break;
+    case F16C: k_convert_shifted<SRC, F16C><<<grid, block, 0, s>>>(src, dst, n, status); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convert_shifted(const void *src, int src_prec, void *dst, int dst_prec, unsigned long long n,
+                                   int *status, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    switch (src_prec) {
+    case F32: return convert_from<F32>(src, dst_prec, dst, n, status, s);
+    case F16S: return convert_from<F16S>(src, dst_prec, dst, n, status, s);
+    case BF16S: return convert_from<BF16S>(src, dst_prec, dst, n, status, s);
+    case F16C: return convert_from<F16C>(src, dst_prec, dst, n, status, s);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 // Halo snapshot entries hold the rest state initially (w_d, or 0 for the shifted forms, whose
 // npol lattice stores f - w_d); the direction of each slot follows the layout documented at k_npol.
 template <int PREC>

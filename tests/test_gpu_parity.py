@@ -395,3 +395,66 @@ def test_shifted_steady_state_against_converged_fp64(plbm, precision, bar):
     mass = abs(float(rho.sum() - rr.sum()) / float(rr.sum()))
     assert l2 <= bar, l2
     assert mass <= 1e-4, mass
+
+
+@pytest.mark.parametrize("alg,lay", [("nptl", "stream"), ("lptl", "bundle"), ("npol", "collision"), ("nsol", "stream")])
+def test_set_precision_continues_the_state_exactly(plbm, alg, lay):
+    """f16s -> f32 re-encodes each stored deviation exactly (the FP16 form's values carry 2^12), and
+    the FP16 form computes on scaled values with the same FP32 operations, so the step after the
+    switch writes the same observables as one more FP16 step; f32 -> f16s -> f32 then continues."""
+    w, h = 157, 53
+    mask = plbm.porous_disks(w, h, 4, 0.7)
+    props = plbm.Properties(alg, lay, False, 64, 10 ** 6, 10 ** 6, "Hagen-Poiseuille", h, w, 0.0, 0.0, 1.02, 0.0, 0.0,
+                            1.0, 0.6)
+    a = plbm.create_handler(props, precision="f16s", mask=mask)
+    b = plbm.create_handler(props, precision="f16s", mask=mask)
+    a.run_steps(301)
+    b.run_steps(300)
+    b.set_precision("f32")
+    assert b.bytes_per_node() == 72.0
+    b.run_steps(1)
+    for get in ("get_densities", "get_x_velocities", "get_y_velocities"):
+        assert np.array_equal(getattr(a, get)(), getattr(b, get)()), get
+    b.set_precision("f16s")
+    b.set_precision("f32")
+    b.run_steps(200)
+    assert np.all(np.isfinite(b.get_densities()))
+    a.close()
+    b.close()
+
+
+def test_set_precision_rejects_forms_outside_the_shifted_ones(plbm):
+    props = plbm.Properties("nptl", "stream", False, 64, 10, 10, "circle", 30, 62, 0.0, 0.0, 1.05, 0.0, 0.0, 1.0, 0.6)
+    hd = plbm.create_handler(props, precision="f64_q60")
+    with pytest.raises(plbm.Exception, match="shifted forms"):
+        hd.set_precision("f32")
+    hd.close()
+    hd = plbm.create_handler(props, precision="f32")
+    with pytest.raises(plbm.Exception, match="shifted forms"):
+        hd.set_precision("f64_strict")
+    hd.set_precision("f32")   # the same form: nothing to do
+    hd.close()
+
+
+def test_escalating_run_reaches_the_target_a_16_bit_form_stalls_above(plbm):
+    """f16s stalls at its rounding floor above residual 1e-6 on this porous channel; finished in
+    FP32 after the stall the same run reaches 1e-6.  Run on towards the steady state, it stays
+    within 2e-3 (relative L2 of j) of the converged FP64 state: the 16-bit rounding left in the slow
+    modes decays only over a long FP32 run (a run stopped at residual 1e-6 is itself ~2e-3 from
+    the steady state), so this bar, not FP32's 3.5e-5, is what the switch guarantees."""
+    w, h = 256, 64
+    mask = plbm.porous_disks(w, h, 12345, 0.7)
+    props = plbm.Properties("nptl", "stream", False, 1024, 10 ** 9, 10 ** 9, "Hagen-Poiseuille", h, w, 0.0, 0.0,
+                            1.01, 0.0, 0.0, 1.0, 0.6)
+    hd = plbm.create_handler(props, precision="f16s", mask=mask)
+    n, r, switched = hd.run_to_residual_escalating(1e-6, 100, 200000)
+    assert r < 1e-6 and switched is not None and switched < n, (n, r, switched)
+    hd.run_to_residual(1e-9, 100, 200000)
+    got = np.concatenate([hd.get_x_velocities(), hd.get_y_velocities()])
+    hd.close()
+    ref_h = plbm.create_handler(props, precision="f64_q60", mask=mask)
+    ref_h.run_to_residual(1e-9, 100, 400000)
+    ref = np.concatenate([ref_h.get_x_velocities(), ref_h.get_y_velocities()])
+    ref_h.close()
+    fl = np.concatenate([mask.reshape(-1) == 0] * 2)
+    assert np.linalg.norm(got[fl] - ref[fl]) / np.linalg.norm(ref[fl]) < 2e-3
