@@ -19,7 +19,8 @@ int plbm_nn_tc_conv(const void *x, const void *w, const float *bias, void *y, in
                     int relu, cudaStream_t s);
 int plbm_nn_tc_flip(const void *w, void *wt, int Cin, int Cout, cudaStream_t s);
 bool plbm_nn_tc_wgrad_supported(int H, int W, int Cin, int Cout);
-int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int W, int Cin, int Cout, cudaStream_t s);
+int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, float *gb, int N, int H, int W, int Cin, int Cout,
+                     int *bias_done, cudaStream_t s);
 bool plbm_nn_tc_small_supported(int H, int W, int Cin, int Cout);
 int plbm_nn_tc_small_conv(const void *x, const void *w, const float *bias, void *y, int N, int H, int W, int Cin,
                           int Cout, int relu, cudaStream_t s);
@@ -519,7 +520,9 @@ int plbm_nn_conv_wgrad(const void *x, const void *g, float *gw, float *gb, int N
 {
     int rc;
     if (plbm_nn_tc_wgrad_supported(H, W, Cin, Cout)) {
-        rc = plbm_nn_tc_wgrad(x, g, gw, N, H, W, Cin, Cout, (cudaStream_t)stream);
+        int bias_done = 0;
+        rc = plbm_nn_tc_wgrad(x, g, gw, gb, N, H, W, Cin, Cout, &bias_done, (cudaStream_t)stream);
+        if (bias_done) gb = nullptr;   // the bias gradient came with the weight gradient
     } else if (plbm_nn_tc_small_wgrad_supported(H, W, Cin, Cout)) {
         rc = plbm_nn_tc_small_wgrad(x, g, gw, N, H, W, Cin, Cout, (cudaStream_t)stream);
     } else {

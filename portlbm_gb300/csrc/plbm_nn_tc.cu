@@ -287,6 +287,8 @@ struct WgArgs {
     int tiles_per_cta, total_tiles;
     int xchunks, gchunks, stage_bytes, stages;
     int g_tma;              // 1: the gradient tiles come by TMA
+    int ones;               // 1: a tile of ones after the input tiles yields the bias gradient
+    float *gb;              // the bias gradient, accumulated when `ones`
     int *err;
 };
 
@@ -340,7 +342,10 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
     int *counts = reinterpret_cast<int *>(tmem_slot + 1);   // [0] issued, [1] consumed, [2] failed
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int npad = a.gchunks * TC_KB, mtiles = (a.xchunks + 3) / 4, blocks = a.ntaps / a.tg;
+    // the stage's M rows: the input tiles, then (ones) a tile whose every value is 1, so its rows
+    // of dW^T are the sums of the gradient over the pixels, i.e. the bias gradient
+    const int xall = a.xchunks + a.ones;
+    const int npad = a.gchunks * TC_KB, mtiles = (xall + 3) / 4, blocks = a.ntaps / a.tg;
     const int used = blocks * mtiles * npad;
     const unsigned ncols = used <= 32 ? 32u : used <= 64 ? 64u : used <= 128 ? 128u : used <= 256 ? 256u : 512u;
     if (threadIdx.x == 0) {
@@ -360,11 +365,17 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
     }
     if (!a.g_tma) {   // the gradient units the writers never touch stay zero
         for (int s = 0; s < a.stages; ++s) {
-            uint4 *z = reinterpret_cast<uint4 *>(smem + s * a.stage_bytes + a.xchunks * WG_CHUNK);
+            uint4 *z = reinterpret_cast<uint4 *>(smem + s * a.stage_bytes + xall * WG_CHUNK);
             for (int i = threadIdx.x; i < a.gchunks * WG_CHUNK / 16; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
+    if (a.ones) {     // bfloat16 1.0 in every element: the swizzle does not matter
+        for (int s = 0; s < a.stages; ++s) {
+            uint4 *o = reinterpret_cast<uint4 *>(smem + s * a.stage_bytes + a.xchunks * WG_CHUNK);
+            for (int i = threadIdx.x; i < WG_CHUNK / 16; i += blockDim.x) o[i] = make_uint4(0x3F803F80u, 0x3F803F80u, 0x3F803F80u, 0x3F803F80u);
+        }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -398,7 +409,7 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
             }
             if (a.g_tma)
                 for (int c = 0; c < a.gchunks; ++c)
-                    tma_load_4d(smem_u32(st + (a.xchunks + c) * WG_CHUNK), &gmap, c * TC_KB, x0, y0, n, bar);
+                    tma_load_4d(smem_u32(st + (xall + c) * WG_CHUNK), &gmap, c * TC_KB, x0, y0, n, bar);
             counts[0] = it + 1;
         }
     } else if (warp == 1 && lane == 0) {       // MMA issuer
@@ -411,11 +422,11 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const unsigned xbase = smem_u32(smem + s * a.stage_bytes), gbase = xbase + (unsigned)(a.xchunks * WG_CHUNK);
+            const unsigned xbase = smem_u32(smem + s * a.stage_bytes), gbase = xbase + (unsigned)(xall * WG_CHUNK);
             const int b = it % blocks;
             const bool first_tile = it < blocks;
             for (int mt = 0; mt < mtiles; ++mt) {
-                const unsigned abase = xbase + (unsigned)(ws_mstart(mt, a.xchunks) * WG_CHUNK);
+                const unsigned abase = xbase + (unsigned)(ws_mstart(mt, xall) * WG_CHUNK);
                 const unsigned dcol = tmem + (unsigned)((b * mtiles + mt) * npad);
 #pragma unroll
                 for (int k = 0; k < TC_BM / 16; ++k)   // K = 16 pixels per MMA: two 8-row groups, 1 KB on
@@ -438,7 +449,7 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
             }
             const int tile = first + it / blocks, n = tile / per_img, t2 = tile % per_img;
             const int y0 = (t2 / a.tiles_x) * a.BH, x0 = (t2 % a.tiles_x) * a.BW;
-            unsigned char *gs = smem + s * a.stage_bytes + a.xchunks * WG_CHUNK;
+            unsigned char *gs = smem + s * a.stage_bytes + xall * WG_CHUNK;
             for (int q = threadIdx.x - 64; q < TC_BM * gunits; q += 64) {
                 const int r = q & (TC_BM - 1), U = q >> 7;
                 *reinterpret_cast<uint4 *>(gs + (U >> 2) * WG_CHUNK + sw64_off(r, U & 3)) =
@@ -458,8 +469,9 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
         const int rows = 9 * a.Cin;
         for (int b = 0; b < blocks; ++b)
             for (int mt = 0; mt < mtiles; ++mt) {
-                const int chunk = ws_mstart(mt, a.xchunks) + warp;   // warp w reads rows 32w .. 32w + 31
-                if (chunk < 4 * mt || chunk >= a.xchunks) continue;   // computed by the previous M tile
+                const int chunk = ws_mstart(mt, xall) + warp;   // warp w reads rows 32w .. 32w + 31
+                if (chunk < 4 * mt || chunk >= xall) continue;   // computed by the previous M tile
+                const bool bias = chunk == a.xchunks;   // the tile of ones: every row holds the bias gradient
                 const int tap = tap0 + b * a.tg + chunk / kbx, row = tap * a.Cin + (chunk % kbx) * TC_KB + lane;
                 for (int c0 = 0; c0 < npad; c0 += 16) {
                     unsigned v[16];
@@ -470,6 +482,13 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
                                  : "r"(taddr));
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                     if (!valid) continue;
+                    if (bias) {   // one lane, one tap group
+                        if (lane == 0 && blockIdx.y == 0 && b == 0)
+#pragma unroll
+                            for (int e = 0; e < 16; ++e)
+                                if (c0 + e < a.Cout) atomicAdd(&a.gb[c0 + e], __uint_as_float(v[e]));
+                        continue;
+                    }
 #pragma unroll
                     for (int e = 0; e < 16; ++e)
                         if (c0 + e < a.Cout) atomicAdd(&a.gw[(size_t)(c0 + e) * rows + row], __uint_as_float(v[e]));
@@ -1105,9 +1124,13 @@ bool plbm_nn_tc_wgrad_supported(int H, int W, int Cin, int Cout)
     return tiles_exactly(H, W);
 }
 
-// gw[co][tap][ci] += sum_p g[p][co] x[p + tap][ci] on the tensor cores (x, g NHWC BF16, gw FP32).
-int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int W, int Cin, int Cout, cudaStream_t s)
+// gw[co][tap][ci] += sum_p g[p][co] x[p + tap][ci] on the tensor cores (x, g NHWC BF16, gw FP32); with
+// gb, also gb[co] += sum_p g[p][co] where a tile of ones fits the stage without another M tile
+// (*bias_done = 1; the caller then runs no bias kernel).
+int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, float *gb, int N, int H, int W, int Cin, int Cout,
+                     int *bias_done, cudaStream_t s)
 {
+    if (bias_done) *bias_done = 0;
     PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
     int *err = error_flag();
     if (!enc || !err) return PLBM_ERR_CUDA;
@@ -1121,10 +1144,12 @@ int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int 
     a.xchunks = a.tg * kbx;
     a.gchunks = (Cout + TC_KB - 1) / TC_KB;
     a.g_tma = Cout % TC_KB == 0;
-    a.stage_bytes = (a.xchunks + a.gchunks) * WG_CHUNK;
     // one CTA per SM with 2-4 stages (two CTAs of one stage each measured slower: each then waits
     // out its own load latency)
     const int budget = 227 * 1024 - WG_SLACK - 1024 - 256;
+    a.gb = gb;
+    a.ones = gb && a.xchunks % 4 != 0 && budget / ((a.xchunks + 1 + a.gchunks) * WG_CHUNK) >= 2 ? 1 : 0;
+    a.stage_bytes = (a.xchunks + a.ones + a.gchunks) * WG_CHUNK;
     a.stages = budget / a.stage_bytes < 4 ? budget / a.stage_bytes : 4;
     if (a.stages < 2) return PLBM_ERR_ARGUMENT;
     a.err = err;
@@ -1161,7 +1186,9 @@ int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, int N, int H, int 
     const int chunks = sms / groups > 0 ? sms / groups : 1;
     a.tiles_per_cta = (a.total_tiles + chunks - 1) / chunks;
     k_wgrad_tc<<<dim3((a.total_tiles + a.tiles_per_cta - 1) / a.tiles_per_cta, groups), 128, smem, s>>>(xmap, gmap, a);
-    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+    if (cudaGetLastError() != cudaSuccess) return PLBM_ERR_CUDA;
+    if (bias_done) *bias_done = a.ones;
+    return PLBM_OK;
 }
 
 // Forward convolution of a narrow input (9 * Cin <= 64, Cout <= 64: eight CTAs of at most 64 TMEM
