@@ -66,9 +66,47 @@ def peaks() -> dict:
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
+class NvmlClocks:
+    """Read-only NVML queries through ctypes (the driver's libnvidia-ml): SM clock, its maximum and
+    the active clock event (throttle) reasons of one GPU.  None of the available() checks fail loudly:
+    without the library the caller falls back to nvidia-smi."""
+
+    # nvmlClocksEventReasons bits, in the order of ClockSampler's reason names
+    REASON_BITS = (0x8, 0x40, 0x20, 0x4)   # hw_slowdown, hw_thermal_slowdown, sw_thermal_slowdown, sw_power_cap
+
+    def __init__(self, index: int):
+        import ctypes
+        self.ct = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit")
+        self.dev = ctypes.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.dev)) != 0:
+            raise OSError("nvmlDeviceGetHandleByIndex")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        v = ctypes.c_uint()
+        self.max_mhz = float(v.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.dev, 1, ctypes.byref(v)) == 0 else 0.0
+
+    def sample(self):
+        """(SM MHz, maximum SM MHz, reason bits) now; NVML_CLOCK_SM is 1."""
+        ct = self.ct
+        v, r = ct.c_uint(), ct.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.dev, 1, ct.byref(v)) != 0:
+            return None
+        if self.reasons_fn(self.dev, ct.byref(r)) != 0:
+            r.value = 0
+        return float(v.value), self.max_mhz, r.value
+
+    def close(self):
+        self.lib.nvmlShutdown()
+
+
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons every `interval_ms` while running; summary()
-    keeps the samples whose nvidia-smi timestamp falls inside the timed steps' wall-clock window."""
+    """Samples the SM clock and the throttle reasons while running: through NVML every millisecond
+    where the library loads (a timed window of 20 steps is ~30 ms), else with nvidia-smi every
+    `interval_ms`; summary() keeps the samples whose timestamp falls inside the timed steps'
+    wall-clock window."""
 
     FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -79,9 +117,26 @@ class ClockSampler:
         self.interval_ms = interval_ms
         self.proc = None
         self.lines: list[str] = []
+        self.nvml_samples: list[tuple] = []
+        self._nvml = None
+        self._stop = threading.Event()
         self._t = None
 
+    def _poll_nvml(self):
+        while not self._stop.is_set():
+            x = self._nvml.sample()
+            if x is not None:
+                self.nvml_samples.append((time.time(),) + x)
+            time.sleep(0.001)
+
     def __enter__(self):
+        try:
+            self._nvml = NvmlClocks(self.index)
+            self._t = threading.Thread(target=self._poll_nvml, daemon=True)
+            self._t.start()
+            return self
+        except Exception:
+            self._nvml = None
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
@@ -97,6 +152,13 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def __exit__(self, *a):
+        self._stop.set()
+        if self._nvml is not None:
+            if self._t:
+                self._t.join(timeout=2)
+            self._nvml.close()
+            self._nvml = None
+            return
         if self.proc:
             self.proc.terminate()
             try:
@@ -108,6 +170,8 @@ class ClockSampler:
 
     def _samples(self):
         import datetime
+        for t, clk, cmax, bits in self.nvml_samples:
+            yield t, clk, cmax, ["Active" if bits & b else "Not Active" for b in NvmlClocks.REASON_BITS]
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:

@@ -46,3 +46,15 @@ def test_reference_arm_samples_a_band_when_the_run_would_be_long(capsys):
     assert line["cpu_baseline"]["sample"].startswith("3 full 256x160 timesteps")
     # the reference arm reports the same config as the measured arm
     assert line["config"] == bench.line_config(args, 1) and line["metric"] == bench.METRIC
+
+
+def test_clock_summary_from_nvml_samples():
+    """The NVML sampler's (time, MHz, max MHz, reason bits) samples go through the same window and
+    reason names as nvidia-smi's lines: bit 0x4 is sw_power_cap, 0x8 hw_slowdown."""
+    c = bench.ClockSampler(0)
+    t0 = 1_790_000_000.0
+    c.nvml_samples = [(t0 + 0.001 * k, 2070.0, 2070.0, 0x4 if k == 5 else 0x1) for k in range(40)]
+    s = c.summary((t0 + 0.0005, t0 + 0.0305))
+    assert s["samples"] == 30 and s["sm_mhz"] == 2070.0 and s["reasons"] == ["sw_power_cap"]
+    c.nvml_samples.append((t0 + 0.02, 1500.0, 2070.0, 0x8))
+    assert "hw_slowdown" in c.summary((t0, t0 + 0.05))["reasons"]
