@@ -758,6 +758,11 @@ def main():
                                                                            lay=args.layout)}
     study = precision_study(plbm) if (rank == 0 and not args.no_study and not args.no_variants) else None
     batch = batch_study(plbm) if (rank == 0 and not args.no_study and not args.no_variants) else None
+    # the warm-start operator's kernels (a few seconds): training step and inference times
+    try:
+        nn = nn_bench() if (rank == 0 and not args.no_study and not args.no_variants) else None
+    except Exception as exc:   # recorded, never fatal to the solver's line
+        nn = {"error": str(exc)[:200]}
 
     # -- CPU baseline (rank 0, N = 1) --
     cpu = None
@@ -795,6 +800,7 @@ def main():
             "variants": variants,
             "precision_study": study,
             "batch_study": batch,
+            "nn_bench": nn,
         }
         print(json.dumps(line), flush=True)
 
