@@ -487,7 +487,8 @@ def sweep(plbm, steps=50, warmup=5, sizes=((2000, 500), (8192, 8192)), taus=(0.5
 def nn_bench(batch=16, size=256, reps=5):
     """Times the warm-start operator's kernels (csrc/plbm_nn.cu): one training step (forward,
     backward, Adam) on `batch` channels of size^2 and one inference of a single channel, with
-    the convolution FLOPs (2 * pixels * 9 * Cin * Cout per layer; backward = 2 x forward)."""
+    the convolution FLOPs (2 * pixels * 9 * Cin * Cout per layer; backward = 2 x forward).
+    Each is timed launched from Python and as a replayed CUDA graph."""
     import numpy as np
     import torch
     from portlbm_gb300 import warmstart as ws
@@ -518,7 +519,7 @@ def nn_bench(batch=16, size=256, reps=5):
         model.adam(lr=0.0)
     e1.record()
     torch.cuda.synchronize()
-    train_ms = e0.elapsed_time(e1) / reps
+    eager_ms = e0.elapsed_time(e1) / reps
     x1 = x[:1].contiguous()
     for it in range(reps + 2):
         if it == 2:
@@ -527,14 +528,33 @@ def nn_bench(batch=16, size=256, reps=5):
         model.forward(x1, 1, size, size)
     e1.record()
     torch.cuda.synchronize()
-    infer_ms = e0.elapsed_time(e1) / reps
+    infer_eager_ms = e0.elapsed_time(e1) / reps
+
+    def replayed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    # the same step and inference as CUDA graphs (one launch from the host each)
+    step = model.capture_train_step(x, grad, batch, size, size)
+    train_ms = replayed(lambda: step(0.0))
+    run, _ = model.capture_forward(x1, 1, size, size)
+    infer_ms = replayed(run)
     pk = peaks()
     train_tf = 3 * flops(batch) / (train_ms * 1e-3) / 1e12
     infer_tf = flops(1) / (infer_ms * 1e-3) / 1e12
     return {"train_step_ms": round(train_ms, 3), "train_tflops": round(train_tf, 2),
             "infer_ms": round(infer_ms, 3), "infer_tflops": round(infer_tf, 2),
+            "train_step_eager_ms": round(eager_ms, 3), "infer_eager_ms": round(infer_eager_ms, 3),
             "bf16_peak_tflops": pk["bf16_tflops"], "train_frac_of_bf16_peak": round(train_tf / pk["bf16_tflops"], 4),
-            "config": f"U-Net 32-128 channels, train batch {batch} x {size}^2, inference 1 x {size}^2"}
+            "config": f"U-Net 32-128 channels, train batch {batch} x {size}^2, inference 1 x {size}^2; "
+                      "train_step_ms / infer_ms replay CUDA graphs, *_eager_ms launch from Python"}
 
 
 def load_traffic(kind: str, nodes: int):

@@ -319,6 +319,11 @@ int plbm_nn_mse(const void *pred, const float *target, const int8_t *mask, void 
                 float inv_count, void *stream);
 int plbm_nn_adam(float *w, const float *g, float *m, float *v, void *w_bf16, long long n, float lr, float b1, float b2,
                  float eps, int t, void *stream);
+/* Adam as plbm_nn_adam with the learning rate read from *lr (device) and the step count kept in
+ * state[0..1] (two device ints, zeroed before the first update): the update uses step state[0] + 1
+ * and stores it, so a launch captured in a CUDA graph advances its own count on every replay. */
+int plbm_nn_adam_dev(float *w, const float *g, float *m, float *v, void *w_bf16, long long n, const float *lr, float b1,
+                     float b2, float eps, int *state, void *stream);
 /* Network input [N,H,W,C] (C >= 4): channel 0 the int8 solid mask, channels 1..3 the per-sample
  * scalars features[3n..3n+2] as constant planes, further channels zero. */
 /* 1 when plbm_nn_conv_fwd runs the shape (input channels Cin, output channels Cout) on tcgen05:

@@ -288,6 +288,38 @@ __global__ void k_adam(float *w, const float *g, float *m, float *v, __nv_bfloat
     }
 }
 
+// Adam with its step count and learning rate on the device, for a launch captured into a CUDA
+// graph: every block reads state[0] = t and updates with step t + 1; the last block to finish
+// (state[1] counts finished blocks) stores t + 1 and clears the count, so each replay advances it.
+__global__ void k_adam_dev(float *w, const float *g, float *m, float *v, __nv_bfloat16 *wb, long long n,
+                           const float *lr_p, float b1, float b2, float eps, int *state)
+{
+    __shared__ bool last;
+    const int t = state[0] + 1;
+    const float lr = *lr_p;
+    const float c1 = 1.f / (1.f - powf(b1, (float)t)), c2 = 1.f / (1.f - powf(b2, (float)t));
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi, vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float wi = w[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+        w[i] = wi;
+        if (wb) wb[i] = __float2bfloat16_rn(wi);
+    }
+    __syncthreads();                       // every thread of the block has read state[0]
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd((unsigned int *)&state[1], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        state[0] = t;
+        state[1] = 0;
+        __threadfence();
+    }
+}
+
 // Network input: channel 0 fluid(0)/solid(1) mask, channels 1..3 the per-sample scalars
 // features[n][0..2] as constant planes; channels beyond 4 are zero.
 __global__ void k_assemble(const int8_t *mask, const float *features, __nv_bfloat16 *y, int N, int H, int W, int C)
@@ -491,16 +523,17 @@ int plbm_nn_conv_dgrad(const void *g, const void *w, void *gx, int N, int H, int
     // the re-laid-out weights in a buffer kept for the process
     const bool tma = plbm_nn_tc_supported(H, W, Cout, Cin);
     if (tma || plbm_nn_tc_small_supported(H, W, Cout, Cin)) {
+        // a buffer that grows is replaced, not freed: a CUDA graph captured earlier may still
+        // launch with the old pointer
         static std::mutex mu;
         static void *wt = nullptr;
         static size_t cap = 0;
         const size_t need = (size_t)Cin * 9 * Cout * 2;
         std::lock_guard<std::mutex> lock(mu);
         if (need > cap) {
-            if (wt) cudaFree(wt);
-            wt = nullptr;
-            cap = 0;
-            if (cudaMalloc(&wt, need) != cudaSuccess) return PLBM_ERR_CUDA;
+            void *p = nullptr;
+            if (cudaMalloc(&p, need) != cudaSuccess) return PLBM_ERR_CUDA;
+            wt = p;
             cap = need;
         }
         const int rc = plbm_nn_tc_flip(w, wt, Cin, Cout, (cudaStream_t)stream);
@@ -632,6 +665,15 @@ int plbm_nn_adam(float *w, const float *g, float *m, float *v, void *wb, long lo
 {
     const float c1 = 1.f / (1.f - powf(b1, (float)t)), c2 = 1.f / (1.f - powf(b2, (float)t));
     k_adam<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(w, g, m, v, (__nv_bfloat16 *)wb, n, lr, b1, b2, eps, c1, c2);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+int plbm_nn_adam_dev(float *w, const float *g, float *m, float *v, void *wb, long long n, const float *lr, float b1,
+                     float b2, float eps, int *state, void *stream)
+{
+    if (n <= 0 || !lr || !state) return PLBM_ERR_ARGUMENT;
+    k_adam_dev<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(w, g, m, v, (__nv_bfloat16 *)wb, n, lr, b1, b2, eps,
+                                                             state);
     return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
 }
 

@@ -276,6 +276,9 @@ k_conv_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUte
 constexpr int WG_M = 128;                          // rows of an M tile (TMEM lanes)
 constexpr int WG_CHUNK = TC_BM * TC_KB * 2;        // one 128-pixel x 32-channel tile, 8 KB
 constexpr int WG_SLACK = 16384;                    // keeps any reading of the descriptors inside the allocation
+constexpr int HALO_ROW = 136;                      // pixels of a halo row x0 - 1 .. x0 + 134 (a multiple of 8)
+constexpr int HALO_ROW_BYTES = 9216;               // HALO_ROW * 64 B rounded up to 1024 B
+constexpr int HALO_STAGE = 3 * HALO_ROW_BYTES;     // three rows of one 32-channel block
 
 struct WgArgs {
     float *gw;
@@ -494,6 +497,176 @@ k_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUt
                         if (c0 + e < a.Cout) atomicAdd(&a.gw[(size_t)(c0 + e) * rows + row], __uint_as_float(v[e]));
                 }
             }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && !valid) {
+        atomicExch(a.err, 1);
+        mbar_wait(smem_u32(done), 0);
+        for (int it = counts[1]; it < counts[0]; ++it)
+            mbar_wait(smem_u32(&full[it % a.stages]), (unsigned)((it / a.stages) & 1));
+    }
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+}
+
+// ---- weight gradient with halo rows (W a multiple of 128) ------------------------------------
+// dW^T as in k_wgrad_tc, but a pixel tile is 128 pixels of one image row and its input comes as the
+// three 136-pixel halo rows (x0 - 1 .. x0 + 134) of each 32-channel block, as in k_conv_halo_tc.
+// An M tile is (dy, channel block): its four 32-row chunks are the taps dx = -1, 0, +1 (and a
+// fourth, dropped) of that halo row, i.e. the same buffer read from 64-byte offsets: the MN-major
+// descriptor's leading byte offset is 64 B (one pixel row), the stride byte offset 512 B per 8
+// pixels, and the 64-byte swizzle follows the address bits.  Per pixel tile 3 x Cin / 32 halo rows
+// (8.5 KB each) and the gradient tile instead of nine shifted tiles per channel block.
+struct WhArgs {
+    float *gw;
+    const __nv_bfloat16 *g;   // read by the writer warps when Cout is not a multiple of 32
+    int N, H, W, Cin, Cout;
+    int tiles_x, total_tiles, tiles_per_cta;
+    int kbx, gchunks, stage_bytes, stages;
+    int g_tma;
+    int *err;
+};
+
+__global__ void __launch_bounds__(128, 1)
+k_wgrad_halo_tc(const __grid_constant__ CUtensorMap hmap, const __grid_constant__ CUtensorMap gmap, WhArgs a)
+{
+    extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+    unsigned char *smem = tc_smem_raw + ((1024 - (smem_u32(tc_smem_raw) & 1023)) & 1023);
+    unsigned long long *bars = reinterpret_cast<unsigned long long *>(smem + a.stages * a.stage_bytes + WG_SLACK);
+    unsigned long long *full = bars, *empty = bars + a.stages, *done = bars + 2 * a.stages;
+    unsigned *tmem_slot = reinterpret_cast<unsigned *>(bars + 2 * a.stages + 1);
+    int *counts = reinterpret_cast<int *>(tmem_slot + 1);   // [0] issued, [1] consumed, [2] failed
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int npad = a.gchunks * TC_KB, mtiles = 3 * a.kbx, used = mtiles * npad;
+    const int rows_bytes = 3 * a.kbx * HALO_ROW_BYTES;   // halo rows of the stage: [dy][kb]
+    const unsigned ncols = used <= 32 ? 32u : used <= 64 ? 64u : used <= 128 ? 128u : used <= 256 ? 256u : 512u;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < a.stages; ++s) {
+            mbar_init(smem_u32(&full[s]), a.g_tma ? 1 : 3);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        mbar_init(smem_u32(done), 1);
+        counts[0] = counts[1] = counts[2] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(ncols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (!a.g_tma) {   // the gradient units the writers never touch stay zero
+        for (int s = 0; s < a.stages; ++s) {
+            uint4 *z = reinterpret_cast<uint4 *>(smem + s * a.stage_bytes + rows_bytes);
+            for (int i = threadIdx.x; i < a.gchunks * WG_CHUNK / 16; i += blockDim.x) z[i] = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = *tmem_slot;
+
+    const int first = blockIdx.x * a.tiles_per_cta;
+    const int iters = max(0, min(a.tiles_per_cta, a.total_tiles - first));
+    const int per_img = a.tiles_x * a.H;
+
+    if (warp == 0 && lane == 0) {              // producer: the halo rows and the g tiles of each pixel tile
+        const unsigned bytes = (unsigned)(rows_bytes / HALO_ROW_BYTES * HALO_ROW * 64 + (a.g_tma ? a.gchunks * WG_CHUNK : 0));
+        for (int it = 0; it < iters; ++it) {
+            const int s = it % a.stages;
+            if (it >= a.stages && !mbar_wait(smem_u32(&empty[s]), (unsigned)((it / a.stages - 1) & 1))) {
+                counts[2] = 1;
+                break;
+            }
+            const int tile = first + it, n = tile / per_img, r = tile % per_img;
+            const int y0 = r / a.tiles_x, x0 = (r % a.tiles_x) * TC_BM;
+            unsigned char *st = smem + s * a.stage_bytes;
+            const unsigned bar = smem_u32(&full[s]);
+            mbar_expect_tx(bar, bytes);
+            for (int dy = 0; dy < 3; ++dy)
+                for (int kb = 0; kb < a.kbx; ++kb)
+                    tma_load_4d(smem_u32(st + (dy * a.kbx + kb) * HALO_ROW_BYTES), &hmap, kb * TC_KB, x0 - 1, y0 + dy - 1,
+                                n, bar);
+            if (a.g_tma)
+                for (int c = 0; c < a.gchunks; ++c)
+                    tma_load_4d(smem_u32(st + rows_bytes + c * WG_CHUNK), &gmap, c * TC_KB, x0, y0, n, bar);
+            counts[0] = it + 1;
+        }
+    } else if (warp == 1 && lane == 0) {       // MMA issuer
+        const unsigned idesc = instr_desc_mn(npad);
+        int it = 0;
+        for (; it < iters; ++it) {
+            const int s = it % a.stages;
+            if (!mbar_wait(smem_u32(&full[s]), (unsigned)((it / a.stages) & 1))) {
+                counts[2] = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const unsigned rbase = smem_u32(smem + s * a.stage_bytes), gbase = rbase + (unsigned)rows_bytes;
+            for (int mt = 0; mt < mtiles; ++mt) {
+                const unsigned abase = rbase + (unsigned)(mt * HALO_ROW_BYTES);
+                const unsigned dcol = tmem + (unsigned)(mt * npad);
+#pragma unroll
+                for (int k = 0; k < TC_BM / 16; ++k)   // K = 16 pixels per MMA: 1 KB on in both operands
+                    umma(dcol, smem_desc_mn_sw64(abase + 1024 * k, 64), smem_desc_mn_sw64(gbase + 1024 * k, WG_CHUNK),
+                         idesc, !(it == 0 && k == 0));
+            }
+            umma_commit(smem_u32(&empty[s]));
+            counts[1] = it + 1;
+        }
+        umma_commit(smem_u32(done));
+    } else if ((warp == 2 || warp == 3) && !a.g_tma) {   // writers of the narrow gradient tiles
+        const int gunits = (a.Cout + 7) / 8;
+        for (int it = 0; it < iters; ++it) {
+            const int s = it % a.stages;
+            bool ok = true;
+            if (lane == 0 && it >= a.stages) ok = mbar_wait(smem_u32(&empty[s]), (unsigned)((it / a.stages - 1) & 1));
+            if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) {
+                if (lane == 0) counts[2] = 1;
+                break;
+            }
+            const int tile = first + it, n = tile / per_img, r = tile % per_img;
+            const int y0 = r / a.tiles_x, x0 = (r % a.tiles_x) * TC_BM;
+            unsigned char *gs = smem + s * a.stage_bytes + rows_bytes;
+            for (int q = threadIdx.x - 64; q < TC_BM * gunits; q += 64) {
+                const int rr = q & (TC_BM - 1), U = q >> 7;
+                *reinterpret_cast<uint4 *>(gs + (U >> 2) * WG_CHUNK + sw64_off(rr, U & 3)) =
+                    pixel_unit(a.g, a.Cout, a.H, a.W, n, y0, x0 + rr, U);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&full[s])) : "memory");
+        }
+    }
+    if (!mbar_wait(smem_u32(done), 0)) counts[2] = 1;
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const bool valid = *((volatile int *)&counts[2]) == 0;
+    if (iters > 0 && warp < 3) {   // warp w: chunk w of each M tile, tap dx = w - 1 (warp 3: the dropped chunk)
+        const int rows = 9 * a.Cin;
+        for (int mt = 0; mt < mtiles; ++mt) {
+            const int dy = mt / a.kbx, kb = mt % a.kbx;
+            const int row = (dy * 3 + warp) * a.Cin + kb * TC_KB + lane;
+            for (int c0 = 0; c0 < npad; c0 += 16) {
+                unsigned v[16];
+                const unsigned taddr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(mt * npad + c0);
+                asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                             : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                               "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                             : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (!valid) continue;
+#pragma unroll
+                for (int e = 0; e < 16; ++e)
+                    if (c0 + e < a.Cout) atomicAdd(&a.gw[(size_t)(c0 + e) * rows + row], __uint_as_float(v[e]));
+            }
+        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -815,9 +988,6 @@ __global__ void __launch_bounds__(WS_THREADS, 2) k_wgrad_small_tc(SmallArgs a)
 // single issuer leaves the tensor pipe idle three quarters of the time at N <= 128.  Warp 0 loads
 // for both, warps 2..5 drain the accumulators in tile order (bias, ReLU, BF16 stores) while the
 // next tiles accumulate.
-constexpr int HALO_ROW = 136;                         // pixels of a halo row (a multiple of 8)
-constexpr int HALO_ROW_BYTES = 9216;                  // HALO_ROW * 64 B rounded up to 1024 B
-constexpr int HALO_STAGE = 3 * HALO_ROW_BYTES;        // three rows of one 32-channel block
 constexpr int HALO_MAX_STAGES = 3;            // per pipeline
 
 struct HaloArgs {
@@ -1134,6 +1304,58 @@ int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, float *gb, int N, 
     PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
     int *err = error_flag();
     if (!enc || !err) return PLBM_ERR_CUDA;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    {   // rows of 128 pixels: the halo-row kernel where its accumulators fit the TMEM
+        const int kbx = Cin / TC_KB, gch = (Cout + TC_KB - 1) / TC_KB;
+        const int hstage = 3 * kbx * HALO_ROW_BYTES + gch * WG_CHUNK;
+        const int hbudget = 227 * 1024 - WG_SLACK - 1024 - 256;
+        const int hst = hbudget / hstage < 4 ? hbudget / hstage : 4;
+        if (W % TC_BM == 0 && 3 * kbx * gch * TC_KB <= 512 && hst >= 2) {
+            WhArgs h{};
+            h.gw = gw; h.g = (const __nv_bfloat16 *)g;
+            h.N = N; h.H = H; h.W = W; h.Cin = Cin; h.Cout = Cout;
+            h.tiles_x = W / TC_BM; h.total_tiles = N * H * h.tiles_x;
+            h.kbx = kbx; h.gchunks = gch; h.stage_bytes = hstage; h.stages = hst;
+            h.g_tma = Cout % TC_KB == 0;
+            h.err = err;
+            h.tiles_per_cta = (h.total_tiles + sms - 1) / sms;
+            const int smem = hst * hstage + WG_SLACK + 1024 + 256;
+            static int hattr = 0;
+            static std::mutex hmu;
+            {
+                std::lock_guard<std::mutex> lk(hmu);
+                if (smem > hattr) {
+                    if (cudaFuncSetAttribute(k_wgrad_halo_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+                        return PLBM_ERR_CUDA;
+                    hattr = smem;
+                }
+            }
+            CUtensorMap hmap, gmap;
+            memset(&gmap, 0, sizeof(gmap));
+            const cuuint32_t es[4] = { 1, 1, 1, 1 };
+            {
+                const cuuint64_t dims[4] = { (cuuint64_t)Cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N };
+                const cuuint64_t strides[3] = { (cuuint64_t)Cin * 2, (cuuint64_t)W * Cin * 2, (cuuint64_t)H * W * Cin * 2 };
+                const cuuint32_t box[4] = { TC_KB, HALO_ROW, 1, 1 };
+                if (enc(&hmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(x), dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                    return PLBM_ERR_ARGUMENT;
+            }
+            if (h.g_tma) {
+                const cuuint64_t dims[4] = { (cuuint64_t)Cout, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N };
+                const cuuint64_t strides[3] = { (cuuint64_t)Cout * 2, (cuuint64_t)W * Cout * 2, (cuuint64_t)H * W * Cout * 2 };
+                const cuuint32_t box[4] = { TC_KB, TC_BM, 1, 1 };
+                if (enc(&gmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(g), dims, strides, box, es,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                    return PLBM_ERR_ARGUMENT;
+            }
+            k_wgrad_halo_tc<<<(h.total_tiles + h.tiles_per_cta - 1) / h.tiles_per_cta, 128, smem, s>>>(hmap, gmap, h);
+            return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+        }
+    }
     WgArgs a{};
     a.gw = gw; a.g = (const __nv_bfloat16 *)g;
     a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout;
@@ -1177,8 +1399,6 @@ int plbm_nn_tc_wgrad(const void *x, const void *g, float *gw, float *gb, int N, 
                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return PLBM_ERR_ARGUMENT;
     }
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
     const int groups = 9 / a.ntaps;
     a.total_tiles = N * a.tiles_x * a.tiles_y;
     // one CTA per SM (the stages fill its shared memory): groups x chunks must not exceed the SMs,

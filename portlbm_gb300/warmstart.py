@@ -58,6 +58,7 @@ def _fns():
         "plbm_nn_add": [vp, vp, vp, ll, vp],
         "plbm_nn_mse": [vp, vp, vp, vp, vp, ll, i, f, vp],
         "plbm_nn_adam": [vp, vp, vp, vp, vp, ll, f, f, f, f, i, vp],
+        "plbm_nn_adam_dev": [vp, vp, vp, vp, vp, ll, vp, f, f, f, vp, vp],
         "plbm_nn_assemble": [vp, vp, vp, i, i, i, i, vp],
     }
     for name, args in sig.items():
@@ -162,6 +163,7 @@ class NeuralOperator:
         self.layers = self.enc + self.dec + [self.head]
         self.norm = np.array([1.0, 1.0])          # std of t_rho and of t_j over the training set
         self.step_count = 0
+        self._s = None
 
     def save(self, path):
         """Writes the FP32 master weights, biases and target scales to an .npz file."""
@@ -183,17 +185,23 @@ class NeuralOperator:
             layer.b.copy_(self.torch.from_numpy(z[f"b{i}"].astype(np.float32)))
         return self
 
+    def _stream(self):
+        """The handle of torch's current CUDA stream (None for the legacy default stream): every
+        kernel of a call goes there, so the calls order with torch's work and can be captured."""
+        return self.torch.cuda.current_stream().cuda_stream or None
+
     def _buf(self, n, h, w, c):
         return self.torch.empty((n, h, w, c), dtype=self.torch.bfloat16, device="cuda")
 
     def _conv(self, layer, x, n, h, w):
         y = self._buf(n, h, w, layer.cout)
         _ok(self.lib.plbm_nn_conv_fwd(x.data_ptr(), layer.wb.data_ptr(), layer.b.data_ptr(), y.data_ptr(), n, h, w,
-                                      layer.cin, layer.cout, int(layer.relu), None))
+                                      layer.cin, layer.cout, int(layer.relu), self._s))
         return y
 
     def forward(self, x, n, h, w):
         """x: [n,h,w,4] bf16 input; returns the [n,h,w,3] prediction and keeps activations for backward."""
+        self._s = self._stream()
         acts = {"in": x}
         cur, hh, ww = x, h, w
         skips = []
@@ -204,7 +212,7 @@ class NeuralOperator:
             skips.append((b, hh, ww))
             if lvl < 4:
                 p = self._buf(n, hh // 2, ww // 2, b.shape[-1])
-                _ok(self.lib.plbm_nn_pool2(b.data_ptr(), p.data_ptr(), n, hh, ww, b.shape[-1], None))
+                _ok(self.lib.plbm_nn_pool2(b.data_ptr(), p.data_ptr(), n, hh, ww, b.shape[-1], self._s))
                 acts[f"p{lvl}"] = p
                 cur, hh, ww = p, hh // 2, ww // 2
             else:
@@ -212,10 +220,10 @@ class NeuralOperator:
         for k, lvl in enumerate((3, 2, 1, 0)):
             sh, sw = skips[lvl][1], skips[lvl][2]
             u = self._buf(n, sh, sw, cur.shape[-1])
-            _ok(self.lib.plbm_nn_up2(cur.data_ptr(), u.data_ptr(), n, sh, sw, cur.shape[-1], None))
+            _ok(self.lib.plbm_nn_up2(cur.data_ptr(), u.data_ptr(), n, sh, sw, cur.shape[-1], self._s))
             a = self._conv(self.dec[2 * k], u, n, sh, sw)
             s = self._buf(n, sh, sw, a.shape[-1])
-            _ok(self.lib.plbm_nn_add(a.data_ptr(), skips[lvl][0].data_ptr(), s.data_ptr(), s.numel(), None))
+            _ok(self.lib.plbm_nn_add(a.data_ptr(), skips[lvl][0].data_ptr(), s.data_ptr(), s.numel(), self._s))
             b = self._conv(self.dec[2 * k + 1], s, n, sh, sw)
             acts[f"u{lvl}"], acts[f"d{lvl}a"], acts[f"s{lvl}"], acts[f"d{lvl}b"] = u, a, s, b
             cur = b
@@ -226,17 +234,18 @@ class NeuralOperator:
 
     def _conv_bwd(self, layer, x, y, gy, n, h, w, need_gx=True):
         if layer.relu:
-            _ok(self.lib.plbm_nn_relu_bwd(y.data_ptr(), gy.data_ptr(), gy.numel(), None))
+            _ok(self.lib.plbm_nn_relu_bwd(y.data_ptr(), gy.data_ptr(), gy.numel(), self._s))
         _ok(self.lib.plbm_nn_conv_wgrad(x.data_ptr(), gy.data_ptr(), layer.gw.data_ptr(), layer.gb.data_ptr(), n, h,
-                                        w, layer.cin, layer.cout, None))
+                                        w, layer.cin, layer.cout, self._s))
         if not need_gx:
             return None
         gx = self._buf(n, h, w, layer.cin)
         _ok(self.lib.plbm_nn_conv_dgrad(gy.data_ptr(), layer.wb.data_ptr(), gx.data_ptr(), n, h, w, layer.cin,
-                                        layer.cout, None))
+                                        layer.cout, self._s))
         return gx
 
     def backward(self, gout):
+        self._s = self._stream()
         a, (n, h, w) = self.acts, self.shape
         g = self._conv_bwd(self.head, a["d0b"], a["out"], gout, n, h, w)
         gskip = {}
@@ -249,15 +258,15 @@ class NeuralOperator:
             gu = self._conv_bwd(self.dec[2 * kk], a[f"u{lvl}"], a[f"d{lvl}a"], gs.clone(), n, sh, sw)
             ch, cw = sizes[lvl + 1]
             g = self._buf(n, ch, cw, gu.shape[-1])
-            _ok(self.lib.plbm_nn_up2_bwd(gu.data_ptr(), g.data_ptr(), n, ch, cw, gu.shape[-1], None))
+            _ok(self.lib.plbm_nn_up2_bwd(gu.data_ptr(), g.data_ptr(), n, ch, cw, gu.shape[-1], self._s))
         for lvl in (4, 3, 2, 1, 0):
             hh, ww = sizes[lvl]
             if lvl < 4:
                 # gradient of e{lvl}b: skip gradient + pooled path gradient
                 gp = self._buf(n, hh, ww, g.shape[-1])
-                _ok(self.lib.plbm_nn_pool2_bwd(g.data_ptr(), gp.data_ptr(), n, hh, ww, g.shape[-1], None))
+                _ok(self.lib.plbm_nn_pool2_bwd(g.data_ptr(), gp.data_ptr(), n, hh, ww, g.shape[-1], self._s))
                 gb_ = self._buf(n, hh, ww, g.shape[-1])
-                _ok(self.lib.plbm_nn_add(gp.data_ptr(), gskip[lvl].data_ptr(), gb_.data_ptr(), gb_.numel(), None))
+                _ok(self.lib.plbm_nn_add(gp.data_ptr(), gskip[lvl].data_ptr(), gb_.data_ptr(), gb_.numel(), self._s))
                 g = gb_
             xin = a["in"] if lvl == 0 else a[f"p{lvl - 1}"]
             ga = self._conv_bwd(self.enc[2 * lvl + 1], a[f"e{lvl}a"], a[f"e{lvl}b"], g, n, hh, ww)
@@ -270,17 +279,72 @@ class NeuralOperator:
         """One Adam update of every weight and bias (one launch over the flat buffers; the padding
         between segments has zero gradients and stays zero)."""
         self.step_count += 1
+        self._s = self._stream()
         p = self.params
         _ok(self.lib.plbm_nn_adam(p.w.data_ptr(), p.g.data_ptr(), p.m.data_ptr(), p.v.data_ptr(), p.wb.data_ptr(),
-                                  p.total, lr, b1, b2, eps, self.step_count, None))
+                                  p.total, lr, b1, b2, eps, self.step_count, self._s))
+
+    def adam_dev(self, lr, state, b1=0.9, b2=0.999, eps=1e-8):
+        """Adam with the learning rate lr ([1] FP32 device tensor) and the step count state ([2]
+        int32 device tensor: the count, and a block counter left at zero) read on the device, so
+        that a captured launch advances the count on each replay."""
+        self._s = self._stream()
+        p = self.params
+        _ok(self.lib.plbm_nn_adam_dev(p.w.data_ptr(), p.g.data_ptr(), p.m.data_ptr(), p.v.data_ptr(), p.wb.data_ptr(),
+                                      p.total, lr.data_ptr(), b1, b2, eps, state.data_ptr(), self._s))
+
+    def capture_train_step(self, x, gout, n, h, w, b1=0.9, b2=0.999, eps=1e-8):
+        """One training step on fixed buffers -- forward on x, zeroed gradients, backward of the
+        output gradient gout, Adam -- captured as a CUDA graph.  Returns step(lr), which sets the
+        learning rate and replays the graph on torch's current stream; new data goes into x and
+        gout in place between replays.  The activations live in the graph's memory pool."""
+        torch = self.torch
+        lr_d = torch.zeros(1, dtype=torch.float32, device="cuda")
+        state = torch.tensor([self.step_count, 0], dtype=torch.int32, device="cuda")
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):          # first calls: kernel attributes, scratch sizes
+            self.forward(x, n, h, w)
+            self.backward(gout)
+            self.zero_grad()
+        torch.cuda.current_stream().wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            self.forward(x, n, h, w)
+            self.zero_grad()
+            self.backward(gout)
+            self.adam_dev(lr_d, state, b1, b2, eps)
+
+        def step(lr):
+            lr_d.fill_(float(lr))
+            graph.replay()
+            self.step_count += 1
+
+        step.graph, step.state, step.out = graph, state, self.acts["out"]
+        return step
+
+    def capture_forward(self, x, n, h, w):
+        """The forward pass on the fixed input buffer x captured as a CUDA graph: returns
+        (run, out), run() replaying it on torch's current stream into the prediction buffer out."""
+        torch = self.torch
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self.forward(x, n, h, w)
+        torch.cuda.current_stream().wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            out = self.forward(x, n, h, w)
+        return graph.replay, out
 
     def assemble(self, masks, feats):
         """masks: [n,h,w] int8 device tensor; feats: n rows of `features` -> [n,h,w,4] bf16 input."""
         torch = self.torch
         n, h, w = masks.shape
+        self._s = self._stream()
         x = self._buf(n, h, w, C_IN)
         f = torch.tensor(np.asarray(feats, dtype=np.float32).reshape(n, 3), device="cuda")
-        _ok(self.lib.plbm_nn_assemble(masks.data_ptr(), f.data_ptr(), x.data_ptr(), n, h, w, C_IN, None))
+        _ok(self.lib.plbm_nn_assemble(masks.data_ptr(), f.data_ptr(), x.data_ptr(), n, h, w, C_IN, self._s))
         return x
 
     def predict(self, mask: np.ndarray, rin: float, rout: float, tau: float, sigma: float = 16.0):
@@ -392,7 +456,7 @@ def train(model: NeuralOperator, samples, epochs=10, batch=16, lr=2e-3, flip=Tru
             loss_d.zero_()
             count = float(fl[sel].sum() * 3)
             _ok(model.lib.plbm_nn_mse(pred.data_ptr(), t.data_ptr(), m.data_ptr(), grad.data_ptr(), loss_d.data_ptr(),
-                                      batch * h * w, 3, 1.0 / count, None))
+                                      batch * h * w, 3, 1.0 / count, model._stream()))
             model.zero_grad()
             model.backward(grad)
             step = ep * (n // batch) + it

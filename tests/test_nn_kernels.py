@@ -105,10 +105,13 @@ def test_tensor_core_convolution(plbm, n, h, w, cin, cout):
 
 
 @pytest.mark.parametrize("n,h,w,cin,cout", [(2, 8, 256, 32, 32), (1, 16, 128, 128, 96), (4, 16, 128, 64, 64),
-                                           (2, 32, 16, 32, 128), (1, 8, 64, 96, 32)])
+                                           (2, 32, 16, 32, 128), (1, 8, 64, 96, 32), (1, 3, 256, 64, 64),
+                                           (2, 4, 384, 32, 3), (1, 2, 128, 64, 32), (1, 5, 128, 96, 32)])
 def test_tensor_core_weight_gradient(plbm, n, h, w, cin, cout):
     """The weight gradient on tcgen05 (both operands MN-major TMA tiles, split over the pixels,
-    FP32 atomics) against the CPU oracle; it accumulates into gw like the other path."""
+    FP32 atomics) against the CPU oracle; it accumulates into gw like the other path.  Rows of a
+    multiple of 128 pixels whose accumulators fit the TMEM run the halo-row form (an M tile's
+    chunks read one halo row at 64-byte offsets), narrow Cout with the gradient written by warps."""
     import torch
     lib = _lib(plbm)
     lib.plbm_nn_status.argtypes = [ctypes.POINTER(ctypes.c_int)]
@@ -196,6 +199,70 @@ def test_pool_and_upsample(plbm):
     # adjoints: <pool(x), y> = <x, pool_bwd(y)> and <up(x), z> = <x, up_bwd(z)>
     _close(_np(gp), nn_ref.up2(_np(p)) / 4.0)
     _close(_np(gu), nn_ref.pool2(x) * 4.0)
+
+
+def test_adam_on_device_matches_host_adam(plbm):
+    """plbm_nn_adam_dev (learning rate and step count read on the device, the count advanced by
+    the launch) gives plbm_nn_adam's update for steps 1..3, and leaves its block counter at zero."""
+    import torch
+    lib = plbm.load_library()
+    vp, ll, f, i = ctypes.c_void_p, ctypes.c_longlong, ctypes.c_float, ctypes.c_int
+    lib.plbm_nn_adam.argtypes = [vp, vp, vp, vp, vp, ll, f, f, f, f, i, vp]
+    lib.plbm_nn_adam_dev.argtypes = [vp, vp, vp, vp, vp, ll, vp, f, f, f, vp, vp]
+    n = 100_003
+    gen = torch.Generator().manual_seed(4)
+    w0, g0 = torch.randn(n, generator=gen), torch.randn(n, generator=gen) * 1e-2
+    bufs = []
+    for _ in range(2):
+        w, g, m, v = w0.cuda(), g0.cuda(), torch.zeros(n, device="cuda"), torch.zeros(n, device="cuda")
+        bufs.append((w, g, m, v, torch.zeros(n, dtype=torch.bfloat16, device="cuda")))
+    lr = torch.tensor([2e-3], device="cuda")
+    state = torch.zeros(2, dtype=torch.int32, device="cuda")
+    for t in (1, 2, 3):
+        w, g, m, v, wb = bufs[0]
+        assert lib.plbm_nn_adam(w.data_ptr(), g.data_ptr(), m.data_ptr(), v.data_ptr(), wb.data_ptr(), n, 2e-3, 0.9,
+                                0.999, 1e-8, t, None) == 0
+        w, g, m, v, wb = bufs[1]
+        assert lib.plbm_nn_adam_dev(w.data_ptr(), g.data_ptr(), m.data_ptr(), v.data_ptr(), wb.data_ptr(), n,
+                                    lr.data_ptr(), 0.9, 0.999, 1e-8, state.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    assert state.tolist() == [3, 0]
+    for a, b in zip(bufs[0], bufs[1]):
+        a, b = a.float(), b.float()
+        assert torch.allclose(a, b, rtol=1e-5, atol=1e-7)
+    assert (bufs[1][0] - w0.cuda()).abs().max().item() > 1e-3     # the weights moved by ~3 lr
+
+
+def test_captured_training_step_matches_eager(plbm):
+    """A training step captured as a CUDA graph (NeuralOperator.capture_train_step) computes the
+    eager step's output bit for bit and its gradients to the weight-gradient tolerance; replays
+    advance the device-held Adam step count and apply the learning rate set before each."""
+    import torch
+    from portlbm_gb300 import warmstart as ws
+    rng = np.random.default_rng(8)
+    n, h, w = 2, 128, 128
+    masks = torch.from_numpy((rng.random((n, h, w)) < 0.3).astype(np.int8)).cuda()
+    gout = _bf(rng.standard_normal((n, h, w, 3)) * 1e-2)
+    eager, graphed = ws.NeuralOperator(seed=6), ws.NeuralOperator(seed=6)
+    x = eager.assemble(masks, [ws.features(w, 1.02, 1.0, 0.8)] * n)
+    out_e = eager.forward(x, n, h, w).clone()
+    eager.zero_grad()
+    eager.backward(gout.clone())
+    torch.cuda.synchronize()
+    w0 = graphed.params.w.clone()
+    step = graphed.capture_train_step(x, gout, n, h, w)
+    step(0.0)
+    torch.cuda.synchronize()
+    assert torch.equal(step.out, out_e)
+    ge, gg = eager.params.g, graphed.params.g
+    assert (ge - gg).abs().max().item() <= 1e-3 * ge.abs().max().item()
+    assert torch.equal(graphed.params.w, w0)                        # lr 0: the weights stay
+    step(1e-3)
+    step(1e-3)
+    torch.cuda.synchronize()
+    assert step.state.tolist() == [3, 0] and graphed.step_count == 3
+    moved = (graphed.params.w - w0).abs().max().item()
+    assert 1e-3 < moved <= 2e-3 * 1.01
 
 
 def test_operator_trains_on_solver_steady_states(plbm):
