@@ -434,15 +434,28 @@ def batch_domains(plbm, n=256, seed=2024):
     return doms
 
 
-def batch_study(plbm, steps=100, precisions=("f32", "f16s"), n=256):
+def parse_batch_tile(text, plbm):
+    """"W,TY,ROWS,BLOCKS[,vec]" -> Batch.set_tile's (tile_w, tile_h, blocks_per_sm)."""
+    parts = text.split(",")
+    w, ty, rows, blocks = (int(v) for v in parts[:4])
+    vec = len(parts) > 4 and parts[4] == "vec"
+    return w, ty + 256 * rows + (plbm.BATCH_TILE_VEC if vec else 0), blocks
+
+
+def batch_study(plbm, steps=100, precisions=("f32", "f16s"), n=256, tile=None):
     """Aggregate MLUPS of `n` uneven domains: one persistent tile-queue launch per step replayed from a
-    CUDA graph (tiles autotuned) against one launch per domain per step."""
+    CUDA graph (tiles autotuned, or `tile` = set_tile's arguments for the 2-byte forms) against one
+    launch per domain per step."""
     doms = batch_domains(plbm, n=n)
     out = {"domains": len(doms)}
     for prec in precisions:
         b = plbm.Batch(doms, precision=prec)
         nodes, _ = b.info()
-        tile = b.autotune(steps=3)
+        if tile is not None and BYTES_PER_NODE[prec] == 36:
+            b.set_tile(*tile)
+            used = tuple(tile)
+        else:
+            used = b.autotune(steps=3)
         _, tiles = b.info()
         b.run(16, mode="persistent_graph")
         ms_graph = b.run(steps, mode="persistent_graph")
@@ -451,9 +464,9 @@ def batch_study(plbm, steps=100, precisions=("f32", "f16s"), n=256):
         ms_per = b.run(steps, mode="per_domain")
         bpn = BYTES_PER_NODE[prec]
         out[prec] = {"nodes": nodes, "tiles": tiles,
-                     "tile": {"threads": [tile[0], tile[1] & 255], "rows_per_thread": max(1, (tile[1] >> 8) & 255),
-                              "vectorised_rows": bool(tile[1] & plbm.BATCH_TILE_VEC),
-                              "blocks_per_sm": tile[2]},
+                     "tile": {"threads": [used[0], used[1] & 255], "rows_per_thread": max(1, (used[1] >> 8) & 255),
+                              "vectorised_rows": bool(used[1] & plbm.BATCH_TILE_VEC),
+                              "blocks_per_sm": used[2], "autotuned": tile is None or BYTES_PER_NODE[prec] != 36},
                      "mlups_persistent_graph": round(nodes / ms_graph / 1e3, 1),
                      "mlups_persistent": round(nodes / ms_pers / 1e3, 1),
                      "mlups_per_domain_launches": round(nodes / ms_per / 1e3, 1),
@@ -680,6 +693,8 @@ def main():
                     help="only the 8192^2 porous precision study, each form run to residual 1e-6 "
                          "with at most CAP steps")
     ap.add_argument("--batch-domains", type=int, default=256)
+    ap.add_argument("--batch-tile", default=None,
+                    help="fixed tile for the 2-byte batch instead of the autotuner: W,THREADS_Y,ROWS,BLOCKS_PER_SM[,vec]")
     ap.add_argument("--nn-bench", action="store_true", help="only the warm-start operator's kernel timings")
     ap.add_argument("--sweep", action="store_true",
                     help="only the FP64 sweep: 4 algorithms x 3 layouts x tau {0.55, 0.6, 1.0} at 2000x500 and 8192^2")
@@ -705,7 +720,9 @@ def main():
                 key, res = "precision_study_large", precision_study(plbm, big_cap=args.precision_study_large,
                                                                     small=False)
             else:
-                key, res = (("batch_study", batch_study(plbm, n=args.batch_domains)) if args.batch_study_only
+                key, res = (("batch_study", batch_study(plbm, n=args.batch_domains,
+                                                          tile=parse_batch_tile(args.batch_tile, plbm)
+                                                          if args.batch_tile else None)) if args.batch_study_only
                             else ("nn_bench", nn_bench()))
             print(json.dumps({key: res}), flush=True)
         return

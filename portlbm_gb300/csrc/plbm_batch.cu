@@ -3,7 +3,7 @@
 // and runs of steps are replayed from a captured CUDA graph.  Each domain keeps its own two
 // lattices (stream layout), links, geometry, relaxation time and boundary densities; the per-node
 // update is the nptl update of plbm_kernels.cuh (FP32, FP16 or BF16 shifted storage, or F64_Q60;
-// the 2-byte forms run the vectorised row update of k_nptl_vec, one warp per 256-node segment).
+// the 2-byte forms can run the vectorised row update, one warp per 256 consecutive nodes).
 //
 // There is no counterpart in the reference, which runs one domain per handler.
 #include "../../include/plbm_c.h"
@@ -82,9 +82,154 @@ __global__ void __launch_bounds__(256, PREC == F64_Q60 ? 3 : 6) k_batch(BatchArg
     }
 }
 
-// 2-byte storage: the same queue, each warp updating 256-node row segments with the vectorised
-// row update of k_nptl_vec_porous (bounce-back merged word-wise, no per-node branches away from the
-// domain edge; blockDim.x == 32; a tile is 256 x (tile_h * tile_rows) nodes).  The
+// An inlet or outlet node of an inner row: its row-loaded values are pull_one's for every direction
+// whose source lies inside the domain, so only the three directions sourced from the ghost column
+// take its constants (x = 0: d = 2, 5, 8 from x = -1; x = W-1: d = 0, 3, 6 from x = W), then the
+// outlet refill -- vec_edge_gather's values without its nine scalar loads.
+template <int PREC>
+__device__ __forceinline__ void vec_edge_column(float *f, int x, int y, const StepParams &p)
+{
+    if (x == 0) {
+        f[2] = g_in<PREC>(p, 2); f[5] = g_in<PREC>(p, 5); f[8] = g_in<PREC>(p, 8);
+    }
+    if (x == p.W - 1) {
+        f[0] = g_out<PREC>(p, 0); f[3] = g_out<PREC>(p, 3); f[6] = g_out<PREC>(p, 6);
+    }
+    if (is_outlet_row(x, y, p)) outlet_fill<PREC>(f, jy_prev_at(p, y), p);
+}
+
+// The porous row update of vec_row_segment_porous with the domain walked in row-major order
+// instead of row by row: the lane owns the eight nodes starting at linear node n0 = y * P + x0
+// (P, the row pitch, is a multiple of 32, so they lie in one row), and a warp's 256 nodes may span
+// rows.  Narrow domains then leave no lanes idle past a row's end.  A lane's neighbour in the warp
+// holds the node before (after) its first (last) node whenever that node is in the same row; where
+// it is not, the node is on the inlet (outlet) column and the direction sourced across the row end
+// is a ghost one, replaced by vec_edge_column.  Every lane takes part in the shuffles; rows 0 and
+// H-1 (edge nodes throughout) keep the scalar gather.  The same values as pull_one.
+template <int PREC>
+__device__ __forceinline__ void vec_linear_segment_porous(const StepParams &p, long long n0, int lane)
+{
+    const long long nodes = (long long)p.P * p.H;
+    const bool vec_ok = n0 < nodes;
+    const long long nc = vec_ok ? n0 : nodes - VEC;             // idle lanes load in range
+    const int y = (int)(nc / p.P), x0 = (int)(nc - (long long)y * p.P);
+    const unsigned short *S = static_cast<const unsigned short *>(p.lat0);
+    const bool inner_row = y > 0 && y < p.H - 1;
+
+    const uint4 l4 = in_range(nc + VEC - 1, p.N, p) ? *reinterpret_cast<const uint4 *>(p.links + nc) : make_uint4(0, 0, 0, 0);
+    const unsigned lw[4] = { l4.x, l4.y, l4.z, l4.w };
+    const bool bounce_here = ((lw[0] | lw[1] | lw[2] | lw[3]) & 0x01EF01EFu) != 0;
+    const bool bounce_warp = __any_sync(0xffffffffu, inner_row && bounce_here);
+    unsigned r[9][4];
+#pragma unroll
+    for (int d = 0; d < 9; ++d) {
+        const size_t at = (size_t)d * p.N + (size_t)(y - cyd(d)) * p.P + x0;
+        const uint4 v = inner_row && in_range(at + VEC - 1, p.lat_elems, p) ? *reinterpret_cast<const uint4 *>(S + at)
+                                                                            : make_uint4(0, 0, 0, 0);
+        r[d][0] = v.x; r[d][1] = v.y; r[d][2] = v.z; r[d][3] = v.w;
+    }
+    unsigned o[6][4];   // own row of planes 0, 1, 2, 6, 7, 8
+    if (bounce_warp) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            const int e = i < 3 ? i : i + 3;
+            const size_t at = (size_t)e * p.N + (size_t)nc;
+            const uint4 v = inner_row && in_range(at + VEC - 1, p.lat_elems, p) ? *reinterpret_cast<const uint4 *>(S + at)
+                                                                                : make_uint4(0, 0, 0, 0);
+            o[i][0] = v.x; o[i][1] = v.y; o[i][2] = v.z; o[i][3] = v.w;
+        }
+    }
+    const unsigned own3[4] = { r[3][0], r[3][1], r[3][2], r[3][3] }, own5[4] = { r[5][0], r[5][1], r[5][2], r[5][3] };
+#pragma unroll
+    for (int d = 0; d < 9; ++d) {
+        const unsigned short *row = S + (size_t)d * p.N + (size_t)(y - cyd(d)) * p.P;
+        if (cxd(d) == 1) {
+            unsigned prev = __shfl_up_sync(0xffffffffu, r[d][3] >> 16, 1);
+            if (lane == 0)
+                prev = inner_row && x0 >= 1 && in_range((size_t)(row - S) + x0 - 1, p.lat_elems, p) ? (unsigned)row[x0 - 1] : 0u;
+            r[d][3] = __byte_perm(r[d][2], r[d][3], 0x5432);
+            r[d][2] = __byte_perm(r[d][1], r[d][2], 0x5432);
+            r[d][1] = __byte_perm(r[d][0], r[d][1], 0x5432);
+            r[d][0] = __byte_perm(prev, r[d][0], 0x5410);
+        } else if (cxd(d) == -1) {
+            unsigned next = __shfl_down_sync(0xffffffffu, r[d][0] & 0xffffu, 1);
+            if (lane == 31)
+                next = inner_row && x0 + VEC < p.P && in_range((size_t)(row - S) + x0 + VEC, p.lat_elems, p)
+                           ? (unsigned)row[x0 + VEC] : 0u;
+            r[d][0] = __byte_perm(r[d][0], r[d][1], 0x5432);
+            r[d][1] = __byte_perm(r[d][1], r[d][2], 0x5432);
+            r[d][2] = __byte_perm(r[d][2], r[d][3], 0x5432);
+            r[d][3] = __byte_perm(r[d][3], next, 0x5432);
+        }
+    }
+    if (bounce_warp) {
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {
+            if (d == 4) continue;
+            const int e = 8 - d;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const unsigned own = e == 3 ? own3[k] : e == 5 ? own5[k] : o[e < 3 ? e : e - 3][k];
+                const unsigned sel = ((lw[k] >> d) & 0x00010001u) * 0xFFFFu;
+                r[d][k] = (r[d][k] & ~sel) | (own & sel);
+            }
+        }
+    }
+    bool over = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float fa[9], fb[9];
+        const uint16_t la = (uint16_t)(lw[k] & 0xffffu), lb = (uint16_t)(lw[k] >> 16);
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {
+            const float sh = cxd(d) != 0 ? p.shift_cx[d] : -0.0f;
+            const float2 v = vec_unpack<PREC>(r[d][k], -0.0f);
+            fa[d] = v.x + (((la >> d) & 1u) ? -0.0f : sh);
+            fb[d] = v.y + (((lb >> d) & 1u) ? -0.0f : sh);
+        }
+        const int xa = x0 + 2 * k, xb = xa + 1;
+        const bool live_a = vec_ok && xa < p.W && (la & LINK_FLUID), live_b = vec_ok && xb < p.W && (lb & LINK_FLUID);
+        if (live_a && (la & LINK_EDGE)) {
+            if (inner_row) vec_edge_column<PREC>(fa, xa, y, p);
+            else vec_edge_gather<PREC>(fa, xa, y, la, p);
+        }
+        if (live_b && (lb & LINK_EDGE)) {
+            if (inner_row) vec_edge_column<PREC>(fb, xb, y, p);
+            else vec_edge_gather<PREC>(fb, xb, y, lb, p);
+        }
+        if (live_a) {
+            const MomentsF m = collide<PREC>(fa, p);
+            emit_observables<PREC>(m, xa, y, p);
+        } else {
+#pragma unroll
+            for (int d = 0; d < 9; ++d) fa[d] = 0.0f;
+        }
+        if (live_b) {
+            const MomentsF m = collide<PREC>(fb, p);
+            emit_observables<PREC>(m, xb, y, p);
+        } else {
+#pragma unroll
+            for (int d = 0; d < 9; ++d) fb[d] = 0.0f;
+        }
+#pragma unroll
+        for (int d = 0; d < 9; ++d) r[d][k] = vec_pack<PREC>(fa[d], fb[d], over);
+    }
+    if constexpr (PREC == F16C)
+        if (over) atomicOr(p.status, 1);
+    if (!vec_ok) return;
+    unsigned short *D = static_cast<unsigned short *>(p.lat1);
+#pragma unroll
+    for (int d = 0; d < 9; ++d) {
+        const size_t at = (size_t)d * p.N + (size_t)nc;
+        if (in_range(at + VEC - 1, p.lat_elems, p))
+            *reinterpret_cast<uint4 *>(D + at) = make_uint4(r[d][0], r[d][1], r[d][2], r[d][3]);
+    }
+}
+
+// 2-byte storage: the same queue, each warp updating 256 consecutive nodes of a domain's row-major
+// order with the vectorised row update of k_nptl_vec_porous (vec_linear_segment_porous: bounce-back
+// merged word-wise, no per-node branches away from the domain edge; blockDim.x == 32; a tile is
+// tile_h * tile_rows such segments).  The
 // queue loop is repeated rather than shared with k_batch through a tile-body lambda: that version
 // compiled k_batch<F32> with more spilled words and ran 1.8 % slower.
 template <int PREC>
@@ -110,12 +255,12 @@ __global__ void __launch_bounds__(256, 2) k_batch_vec(BatchArgs a)
             __syncthreads();
             cur = dom;
         }
-        const int local = (int)a.tile_local[t], txs = a.tiles_x[dom];
-        const int xv = (local % txs) * (32 * VEC) + threadIdx.x * VEC;
-        const int y0 = (local / txs) * a.tile_h * a.tile_rows + threadIdx.y;
+        // tile `local` is segments local * S .. local * S + S - 1 of the domain's row-major node order
+        const long long seg0 = (long long)a.tile_local[t] * (a.tile_h * a.tile_rows) + threadIdx.y;
+        const long long nodes = (long long)sp.P * sp.H;
         for (int r = 0; r < a.tile_rows; ++r) {
-            const int yi = y0 + r * a.tile_h;
-            if (yi < sp.H) vec_row_segment_porous<PREC>(sp, yi, xv, threadIdx.x);   // uniform over the warp
+            const long long base = (seg0 + (long long)r * a.tile_h) * (32 * VEC);
+            if (base < nodes) vec_linear_segment_porous<PREC>(sp, base + threadIdx.x * VEC, threadIdx.x);   // warp-uniform
         }
         if (tid == 0) s_tile = next;
         __syncthreads();
@@ -191,8 +336,12 @@ struct plbm_batch {
         std::vector<int> tx;
         for (unsigned i = 0; i < n_domains(); ++i) {
             const StepParams &d = host[2 * i];
+            // vectorised rows: tiles of tile_h * tile_rows 256-node segments of the row-major order
+            const long long segs = ((long long)d.P * d.H + 32 * plbm::VEC - 1) / (32 * plbm::VEC);
             const int tw = tile_nodes_w();
-            const int nx = (d.W + tw - 1) / tw, ny = (d.H + tile_h * tile_rows - 1) / (tile_h * tile_rows);
+            const int nx = vec() ? 1 : (d.W + tw - 1) / tw;
+            const int ny = vec() ? (int)((segs + tile_h * tile_rows - 1) / (tile_h * tile_rows))
+                                 : (d.H + tile_h * tile_rows - 1) / (tile_h * tile_rows);
             tx.push_back(nx);
             for (int k = 0; k < nx * ny; ++k) { dom.push_back(i); loc.push_back((unsigned)k); }
         }

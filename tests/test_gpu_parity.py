@@ -334,6 +334,34 @@ def test_batch_equals_independent_handlers(plbm, precision, mode, wide, vec_rows
     b.close()
 
 
+@pytest.mark.parametrize("precision", ["f16s", "bf16s", "f16c"])
+def test_batch_vectorised_rows_across_row_ends(plbm, precision):
+    """The vectorised batch walks each domain in row-major order, 256 nodes per warp, so a warp's
+    lanes span rows: widths that are multiples of 32 end a row exactly at a lane (its neighbour lane
+    starts the next row), and node counts that are not multiples of 256 leave a partial last
+    segment.  Every domain still ends bit-identical to the channel run alone."""
+    rng = np.random.default_rng(23)
+    doms = []
+    for i, (w, h) in enumerate(((32, 24), (64, 25), (96, 31), (256, 17), (40, 29), (72, 9), (288, 40))):
+        doms.append({"mask": plbm.porous_disks(w, h, 40 + i, 0.75), "relaxation_time": float(rng.uniform(0.55, 1.0)),
+                     "inlet_density": float(rng.uniform(1.001, 1.05)), "outlet_density": 1.0})
+    b = plbm.Batch(doms, precision=precision)
+    b.set_tile(32, 2 + 256 * 2 + plbm.BATCH_TILE_VEC, 4)
+    steps = 120
+    b.run(steps, mode="persistent_graph")
+    for i, d in enumerate(doms):
+        h, w = d["mask"].shape
+        props = plbm.Properties("nptl", "stream", False, 64, steps, steps, "Hagen-Poiseuille", h, w, 0.0, 0.0,
+                                d["inlet_density"], 0.0, 0.0, 1.0, d["relaxation_time"])
+        hd = plbm.create_handler(props, precision=precision, mask=d["mask"])
+        hd.start()
+        hd.block_until_finished()
+        for k, get in enumerate((hd.get_densities, hd.get_x_velocities, hd.get_y_velocities)):
+            assert np.array_equal(b.result(i, k), get()), (i, k)
+        hd.close()
+    b.close()
+
+
 @pytest.mark.parametrize("precision", ["f32", "f16s", "f16c"])
 def test_batch_autotune_keeps_results(plbm, precision):
     """Autotuning times real steps (7 tile shapes x 3 occupancies x 2 steps, twice that for 2-byte
