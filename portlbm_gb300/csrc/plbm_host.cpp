@@ -473,6 +473,8 @@ struct plbm_handler {
     unsigned export_fields = 0;  // bit i: result i (PLBM_DENSITY ..)
     double *res_h[4] = { nullptr, nullptr, nullptr, nullptr };
     double *res_hd[4] = { nullptr, nullptr, nullptr, nullptr };   // device addresses of res_h
+    // a result step wrote res_h through res_hd (the step loop's frames): res_d is older than res_h
+    std::atomic<bool> host_results_newer{ false };
     size_t res_h_bytes = 0;
     bool res_h_registered = false;
     // The host result arrays are allocated, first touched with their initial values by parallel
@@ -932,23 +934,27 @@ struct plbm_handler {
         }
     }
 
+    // The host arrays take the newest results: copied from res_d, unless a step already wrote them.
     void copy_results()
     {
         wait_host();
-        for (int i = 0; i < 4; ++i)
-            cuda_check(cudaMemcpyAsync(res_h[i], res_d[i], nres * sizeof(double), cudaMemcpyDeviceToHost, stream),
-                       "D2H results");
+        if (!host_results_newer.load())
+            for (int i = 0; i < 4; ++i)
+                cuda_check(cudaMemcpyAsync(res_h[i], res_d[i], nres * sizeof(double), cudaMemcpyDeviceToHost, stream),
+                           "D2H results");
         cuda_check(cudaStreamSynchronize(stream), "results copy");
     }
 
-    // Frame copies on the stream, without waiting (the host arrays are refreshed when the copy
-    // lands, as a reader of the reference's unsynchronised getters would observe).
-    void enqueue_results_copy()
+    // res_d takes the newest results back from the host arrays where a step wrote those instead.
+    void device_results_current()
     {
+        if (!host_results_newer.load()) return;
         wait_host();
         for (int i = 0; i < 4; ++i)
-            cuda_check(cudaMemcpyAsync(res_h[i], res_d[i], nres * sizeof(double), cudaMemcpyDeviceToHost, stream),
-                       "D2H results");
+            cuda_check(cudaMemcpyAsync(res_d[i], res_h[i], nres * sizeof(double), cudaMemcpyHostToDevice, stream),
+                       "H2D results");
+        cuda_check(cudaStreamSynchronize(stream), "results copy");
+        host_results_newer = false;
     }
 
     // The per-step loop of the drivers (nptl.hpp:121-139): stop when paused or finished; results
@@ -983,14 +989,19 @@ struct plbm_handler {
                 if (opt.use_graph && !export_fields && !debug && F >= 2 && F <= 256 && t % F == 0 && t + F < T) {
                     // a whole frame: one graph launch (its steps, results written to the host)
                     cuda_check(cudaGraphLaunch(frame_graph(t, F), stream), "frame graph launch");
+                    host_results_newer = true;
                     end = t + F;
                 } else if (t < frame) {
                     const unsigned chunk = std::max<unsigned>(graph_steps ? graph_steps : 32, 32);
                     end = std::min(frame, t + chunk);
                     run_plain(t, end);
                 } else {
-                    cuda_check(launch_step(t, true), "step");
-                    enqueue_results_copy();
+                    // a frame step writes its observables into the mapped host arrays itself (no
+                    // copy after it; a reader of the reference's unsynchronised getters sees the
+                    // arrays refreshed while the step runs)
+                    wait_host();
+                    cuda_check(launch_step(t, true, true), "step");
+                    host_results_newer = true;
                     end = t + 1;
                     if (export_fields) {
                         publish(end);
@@ -1258,6 +1269,7 @@ int plbm_run_steps(plbm_handler *h, unsigned n, double *ms_per_step)
         cuda_check(cudaEventRecord(h->ev0, h->stream), "event");
         h->run_plain(t0, t0 + n - 1);
         cuda_check(h->launch_step(t0 + n - 1, true), "step");
+        h->host_results_newer = false;
         cuda_check(cudaEventRecord(h->ev1, h->stream), "event");
         cuda_check(cudaEventSynchronize(h->ev1), "steps");
         float ms = 0;
@@ -1506,6 +1518,7 @@ int plbm_bytes_per_node(plbm_handler *h, double *bytes)
 int plbm_mass_momentum(plbm_handler *h, double out3[3])
 {
     return guarded(h, [&] {
+        h->device_results_current();
         cuda_check(plbm::launch_reduce_results(h->res_d[0], h->res_d[1], h->res_d[2], h->flags_d, h->nres, h->red_d,
                                                h->stream),
                    "reduce");
