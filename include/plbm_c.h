@@ -310,6 +310,9 @@ int plbm_nn_conv_dgrad(const void *g, const void *w, void *gx, int N, int H, int
 int plbm_nn_conv_wgrad(const void *x, const void *g, float *gw, float *gb, int N, int H, int W, int Cin, int Cout,
                        void *stream);
 int plbm_nn_relu_bwd(const void *y, void *g, long long n, void *stream);
+/* The ReLU backward of g ([P, C] bfloat16, in place: g = g where y > 0, else 0) together with the
+ * bias gradient gb[c] += sum over the P pixels of the masked g[p][c] (FP32), in one pass over g. */
+int plbm_nn_relu_bwd_bias(const void *y, void *g, float *gb, long long P, int C, void *stream);
 int plbm_nn_pool2(const void *x, void *y, int N, int H, int W, int C, void *stream);
 int plbm_nn_pool2_bwd(const void *gy, void *gx, int N, int H, int W, int C, void *stream);
 int plbm_nn_up2(const void *x, void *y, int N, int H, int W, int C, void *stream);

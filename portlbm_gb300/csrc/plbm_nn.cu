@@ -354,18 +354,39 @@ __device__ __forceinline__ uint4 pack8(const float f[8])
     return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
+// Eight bfloat16 gradients kept where y > 0 (a positive, non-NaN bfloat16), zeroed elsewhere.
+__device__ __forceinline__ uint4 relu_mask8(uint4 yv, uint4 gv)
+{
+    uint32_t *gw = reinterpret_cast<uint32_t *>(&gv);
+    const uint32_t yw[4] = { yv.x, yv.y, yv.z, yv.w };
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const bool lo = __uint_as_float(yw[k] << 16) > 0.f, hi = __uint_as_float(yw[k] & 0xffff0000u) > 0.f;
+        gw[k] &= (lo ? 0x0000ffffu : 0u) | (hi ? 0xffff0000u : 0u);
+    }
+    return gv;
+}
+
 // gb[c] += sum over the P pixels of g[p][c]: thread (pixel lane q, unit u) of a block of
 // R = blockDim.x / CU pixel lanes sums unit u of every (R * gridDim.x)-th pixel; the block's lanes
-// are then added per channel in shared memory, one atomic per channel and block.
-__global__ void k_bias_grad_v(const uint4 *g, float *gb, unsigned P, int CU)
+// are then added per channel in shared memory, one atomic per channel and block.  RELU: the ReLU
+// backward first, in place (g = g * (y > 0)), and the masked values summed: one pass over g.
+template <bool RELU>
+__global__ void k_bias_grad_v(const uint4 *y, uint4 *g, float *gb, unsigned P, int CU)
 {
     extern __shared__ float red[];
     const int R = blockDim.x / CU, q = threadIdx.x / CU, u = threadIdx.x - q * CU;
     float s[8] = { 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f };
     if (q < R)
         for (unsigned p = blockIdx.x * (unsigned)R + q; p < P; p += gridDim.x * (unsigned)R) {
+            const size_t i = (size_t)p * CU + u;
+            uint4 gv = g[i];
+            if constexpr (RELU) {
+                gv = relu_mask8(y[i], gv);
+                g[i] = gv;
+            }
             float f[8];
-            unpack8(g[(size_t)p * CU + u], f);
+            unpack8(gv, f);
 #pragma unroll
             for (int e = 0; e < 8; ++e) s[e] += f[e];
         }
@@ -382,18 +403,7 @@ __global__ void k_bias_grad_v(const uint4 *g, float *gb, unsigned P, int CU)
 
 __global__ void k_relu_bwd_v(const uint4 *y, uint4 *g, unsigned n8)
 {
-    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += gridDim.x * blockDim.x) {
-        const uint4 yv = y[i];
-        uint4 gv = g[i];
-        uint32_t *gw = reinterpret_cast<uint32_t *>(&gv);
-        const uint32_t yw[4] = { yv.x, yv.y, yv.z, yv.w };
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {   // keep the gradient where y > 0 (a positive, non-NaN bfloat16)
-            const bool lo = __uint_as_float(yw[k] << 16) > 0.f, hi = __uint_as_float(yw[k] & 0xffff0000u) > 0.f;
-            gw[k] &= (lo ? 0x0000ffffu : 0u) | (hi ? 0xffff0000u : 0u);
-        }
-        g[i] = gv;
-    }
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n8; i += gridDim.x * blockDim.x) g[i] = relu_mask8(y[i], g[i]);
 }
 
 __global__ void k_add_v(const uint4 *a, const uint4 *b, uint4 *y, unsigned n8)
@@ -485,6 +495,28 @@ bool vec8(int C, long long elems, const void *a, const void *b = nullptr, const 
     return C % 8 == 0 && elems % 8 == 0 && elems / 8 < (1ll << 31) && al(a) && al(b) && al(c);
 }
 
+// gb[c] += sum over the P pixels of g[p][c]; with y, the ReLU backward of g first, in place (the
+// 16-byte kernel needs C a multiple of 8 and aligned buffers; y without them is applied by the caller).
+int bias_grad(const void *y, void *g, float *gb, long long P, int C, cudaStream_t s)
+{
+    if (vec8(C, P * C, g, y)) {
+        const int CU = C / 8, threads = (256 / CU) * CU;
+        const long long R = threads / CU;
+        const int blocks = (int)((P + R - 1) / R < 152 * 4 ? (P + R - 1) / R : 152 * 4);
+        if (y)
+            k_bias_grad_v<true><<<blocks, threads, threads * 8 * sizeof(float), s>>>((const uint4 *)y, (uint4 *)g, gb,
+                                                                                   (unsigned)P, CU);
+        else
+            k_bias_grad_v<false><<<blocks, threads, threads * 8 * sizeof(float), s>>>(nullptr, (uint4 *)g, gb,
+                                                                                    (unsigned)P, CU);
+        return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+    }
+    const long long gx = (P + 7) / 8 < 1024 ? (P + 7) / 8 : 1024;
+    dim3 grid((unsigned)gx, (unsigned)((C + 31) / 32));
+    k_bias_grad<<<grid, 256, 0, s>>>((const __nv_bfloat16 *)g, gb, P, C);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
 template <int MODE>
 int run_conv(ConvArgs a, cudaStream_t s)
 {
@@ -565,21 +597,20 @@ int plbm_nn_conv_wgrad(const void *x, const void *g, float *gw, float *gb, int N
         a.M = Cout; a.Ncols = 9 * Cin; a.K = N * H * W;
         rc = run_conv<WGRAD>(a, (cudaStream_t)stream);
     }
-    if (rc == PLBM_OK && gb && vec8(Cout, (long long)N * H * W * Cout, g)) {
-        const int CU = Cout / 8, threads = (256 / CU) * CU;
-        const long long P = (long long)N * H * W, R = threads / CU;
-        const int blocks = (int)((P + R - 1) / R < 152 * 4 ? (P + R - 1) / R : 152 * 4);
-        k_bias_grad_v<<<blocks, threads, threads * 8 * sizeof(float), (cudaStream_t)stream>>>(
-            (const uint4 *)g, gb, (unsigned)P, CU);
-        rc = cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
-    } else if (rc == PLBM_OK && gb) {
-        const long long P = (long long)N * H * W;
-        const long long gx = (P + 7) / 8 < 1024 ? (P + 7) / 8 : 1024;
-        dim3 grid((unsigned)gx, (unsigned)((Cout + 31) / 32));
-        k_bias_grad<<<grid, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)g, gb, P, Cout);
-        rc = cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
-    }
+    // without y the bias kernel only reads g
+    if (rc == PLBM_OK && gb)
+        rc = bias_grad(nullptr, const_cast<void *>(g), gb, (long long)N * H * W, Cout, (cudaStream_t)stream);
     return rc;
+}
+
+int plbm_nn_relu_bwd_bias(const void *y, void *g, float *gb, long long P, int C, void *stream)
+{
+    if (P <= 0 || C <= 0 || !gb) return PLBM_ERR_ARGUMENT;
+    if (!vec8(C, P * C, y, g)) {
+        const int rc = plbm_nn_relu_bwd(y, g, P * C, stream);
+        return rc == PLBM_OK ? bias_grad(nullptr, g, gb, P, C, (cudaStream_t)stream) : rc;
+    }
+    return bias_grad(y, g, gb, P, C, (cudaStream_t)stream);
 }
 
 int plbm_nn_relu_bwd(const void *y, void *g, long long n, void *stream)

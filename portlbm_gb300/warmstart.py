@@ -51,6 +51,7 @@ def _fns():
         "plbm_nn_conv_dgrad": [vp, vp, vp, i, i, i, i, i, vp],
         "plbm_nn_conv_wgrad": [vp, vp, vp, vp, i, i, i, i, i, vp],
         "plbm_nn_relu_bwd": [vp, vp, ll, vp],
+        "plbm_nn_relu_bwd_bias": [vp, vp, vp, ll, i, vp],
         "plbm_nn_pool2": [vp, vp, i, i, i, i, vp],
         "plbm_nn_pool2_bwd": [vp, vp, i, i, i, i, vp],
         "plbm_nn_up2": [vp, vp, i, i, i, i, vp],
@@ -233,10 +234,12 @@ class NeuralOperator:
         return out
 
     def _conv_bwd(self, layer, x, y, gy, n, h, w, need_gx=True):
-        if layer.relu:
-            _ok(self.lib.plbm_nn_relu_bwd(y.data_ptr(), gy.data_ptr(), gy.numel(), self._s))
-        _ok(self.lib.plbm_nn_conv_wgrad(x.data_ptr(), gy.data_ptr(), layer.gw.data_ptr(), layer.gb.data_ptr(), n, h,
-                                        w, layer.cin, layer.cout, self._s))
+        gb = layer.gb.data_ptr()
+        if layer.relu:   # the ReLU backward and the bias gradient in one pass over the gradient
+            _ok(self.lib.plbm_nn_relu_bwd_bias(y.data_ptr(), gy.data_ptr(), gb, n * h * w, layer.cout, self._s))
+            gb = None
+        _ok(self.lib.plbm_nn_conv_wgrad(x.data_ptr(), gy.data_ptr(), layer.gw.data_ptr(), gb, n, h, w, layer.cin,
+                                        layer.cout, self._s))
         if not need_gx:
             return None
         gx = self._buf(n, h, w, layer.cin)

@@ -201,6 +201,30 @@ def test_pool_and_upsample(plbm):
     _close(_np(gu), nn_ref.pool2(x) * 4.0)
 
 
+@pytest.mark.parametrize("p,c", [(4096, 32), (3000, 96), (777, 128), (500, 12)])
+def test_relu_backward_with_bias_gradient(plbm, p, c):
+    """plbm_nn_relu_bwd_bias masks the gradient where the activation is not positive (bit-exact) and
+    adds the masked gradient's per-channel sums to gb (FP32 sums: 1e-4 relative); c = 12 runs the
+    element-wise fallback."""
+    import torch
+    lib = plbm.load_library()
+    vp, ll, i = ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int
+    lib.plbm_nn_relu_bwd_bias.argtypes = [vp, vp, vp, ll, i, vp]
+    rng = np.random.default_rng(p + c)
+    y = nn_ref.bf16_round(rng.standard_normal((p, c)))
+    y[rng.random((p, c)) < 0.05] = 0.0
+    g = nn_ref.bf16_round(rng.standard_normal((p, c)))
+    yd, gd = _bf(y), _bf(g)
+    gb0 = rng.standard_normal(c).astype(np.float32)
+    gb = torch.from_numpy(gb0.copy()).cuda()
+    assert lib.plbm_nn_relu_bwd_bias(yd.data_ptr(), gd.data_ptr(), gb.data_ptr(), p, c, None) == 0
+    torch.cuda.synchronize()
+    masked = np.where(y > 0, g, 0.0)
+    assert np.array_equal(_np(gd), masked)
+    ref = gb0.astype(np.float64) + masked.sum(axis=0)
+    assert np.max(np.abs(gb.cpu().numpy() - ref)) <= 1e-4 * np.max(np.abs(masked).sum(axis=0)) + 1e-5
+
+
 def test_adam_on_device_matches_host_adam(plbm):
     """plbm_nn_adam_dev (learning rate and step count read on the device, the count advanced by
     the launch) gives plbm_nn_adam's update for steps 1..3, and leaves its block counter at zero."""
