@@ -792,6 +792,10 @@ struct plbm_handler {
                 bx = std::min(bx, (unsigned)W);
                 by = std::min(by, (unsigned)H);
             }
+            if (alg == 3 && lay == plbm::COLLISION) {   // nsol records: 32 x 8 tiles stage the even step's stores
+                bx = 32;
+                by = (unsigned)plbm::NSOL_STAGE_ROWS;
+            }
             block = dim3(bx, by);
             grid = dim3((W + bx - 1) / bx, (H + by * ny - 1) / (by * ny));
         }

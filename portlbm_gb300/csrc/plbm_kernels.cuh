@@ -16,6 +16,7 @@
 #pragma once
 
 #include "plbm_device.cuh"
+#include "plbm_launch.h"
 
 namespace plbm {
 
@@ -681,18 +682,13 @@ __global__ void __launch_bounds__(NptlBounds<PREC>::threads, NptlBounds<PREC>::b
 //   state Q (before an odd step):  slot (m, k) holds the value arriving at m along k.
 // The initial rest state is both (weights are symmetric, w_k = w_{8-k}).
 
+// The even-step gather of a fluid node: each source neighbour's reversed slot, the node's own slot
+// behind a solid, ghost constants at the domain edge.
 template <int PREC, int L>
-__global__ void k_nsol_even(StepParams p)
+__device__ __forceinline__ void nsol_even_gather(CT<PREC> f[9], unsigned long long n, int xi, int yi, uint16_t lk,
+                                                 const StepParams &p)
 {
-    const int xi = blockIdx.x * blockDim.x + threadIdx.x;
-    const int yi = blockIdx.y * blockDim.y + threadIdx.y;
-    if (xi >= p.W || yi >= p.H) return;
-    const unsigned long long n = (unsigned long long)xi + (unsigned long long)yi * p.P;
-    const uint16_t lk = link_at(p, n);
-    if (!(lk & LINK_FLUID)) return;
-    CT<PREC> f[9];
-    const bool fast = lk == LINK_FLUID;   // links carry LINK_EDGE on the domain edge
-    if (fast) {
+    if (lk == LINK_FLUID) {   // links carry LINK_EDGE on the domain edge
 #pragma unroll
         for (int d = 0; d < 9; ++d) f[d] = ld<PREC>(p.lat0, lidx<L>(n, 8 - d, p.N) + pull_delta<L>(d, p), 8 - d, p);
     } else {
@@ -711,6 +707,80 @@ __global__ void k_nsol_even(StepParams p)
             }
         }
     }
+}
+
+// nsol's even step in the collision (record) layout with its stores staged per block.  A node
+// writes value d into slot d of neighbour n + c_d, so written one by one a warp's stores sit 72
+// bytes apart and each fills an eighth or a quarter of a sector.  A 32-wide tile of up to
+// NSOL_STAGE_ROWS rows has every slot of each of its own records written by its own nodes: the
+// block places each new value in a shared-memory copy of the tile's records and their one-node
+// frame (with a flag per slot), and after one barrier writes the copy out row by row, consecutive
+// threads on consecutive entries, the flagged slots only (the frame's records are shared with the
+// neighbouring tiles; slots toward a ghost are never written).  Every slot a node writes is one
+// it read itself (the AA pattern), so no other block reads it in this step.
+template <int PREC>
+__device__ __forceinline__ void nsol_even_collision_staged(const StepParams &p)
+{
+    using T = typename Store<PREC>::T;
+    constexpr int RW = 34, RH = NSOL_STAGE_ROWS + 2, E = RW * 9;   // entries per frame row
+    __shared__ T stage[RH * E];
+    __shared__ unsigned char written[RH * E];
+    const int tid = threadIdx.y * 32 + threadIdx.x, nt = 32 * blockDim.y, rows = blockDim.y + 2;
+    for (int i = tid; i < rows * E; i += nt) written[i] = 0;
+    __syncthreads();
+    const int xi = blockIdx.x * 32 + threadIdx.x, yi = blockIdx.y * blockDim.y + threadIdx.y;
+    const bool inside = xi < p.W && yi < p.H;
+    const unsigned long long n = inside ? (unsigned long long)xi + (unsigned long long)yi * p.P : 0;
+    const uint16_t lk = inside ? link_at(p, n) : 0;
+    if (lk & LINK_FLUID) {
+        CT<PREC> f[9];
+        nsol_even_gather<PREC, COLLISION>(f, n, xi, yi, lk, p);
+        if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, jy_prev_at(p, yi), p);
+        const auto m = collide<PREC>(f, p);
+#pragma unroll
+        for (int d = 0; d < 9; ++d) {
+            const int tx = xi + cxd(d), ty = yi + cyd(d);
+            if (tx < 0 || tx >= p.W || ty < 0 || ty >= p.H) continue;   // toward a ghost: never read
+            const int i = (threadIdx.y + 1 + cyd(d)) * E + (threadIdx.x + 1 + cxd(d)) * 9 + d;
+            stage[i] = encode_value<PREC>(f[d], p);
+            written[i] = 1;
+        }
+        emit_observables<PREC>(m, xi, yi, p);
+    }
+    __syncthreads();
+    // frame row r is lattice row y0 - 1 + r, records x0 - 1 .. x0 + 32: 306 consecutive entries
+    const long long x0 = (long long)blockIdx.x * 32, y0 = (long long)blockIdx.y * blockDim.y;
+    T *lat = static_cast<T *>(p.lat0);
+    for (int i = tid; i < rows * E; i += nt) {
+        if (!written[i]) continue;                                      // flagged slots lie in the domain
+        const int r = i / E, k = i - r * E;
+        const unsigned long long e = 9ull * ((unsigned long long)(y0 - 1 + r) * p.P + (unsigned long long)(x0 - 1)) + k;
+        if (in_range(e, p.lat_elems, p)) lat[e] = stage[i];
+    }
+}
+
+// The Q60 form's staged even step in the collision layout runs a fifth resident 256-thread block.
+template <int PREC, int L> struct NsolEvenBlocks { static constexpr int value = 1; };
+template <> struct NsolEvenBlocks<F64_Q60, COLLISION> { static constexpr int value = 5; };
+
+template <int PREC, int L>
+__global__ void __launch_bounds__(256, NsolEvenBlocks<PREC, L>::value) k_nsol_even(StepParams p)
+{
+    if constexpr (L == COLLISION) {
+        if (blockDim.x == 32 && blockDim.y <= NSOL_STAGE_ROWS) {   // uniform over the grid
+            nsol_even_collision_staged<PREC>(p);
+            return;
+        }
+    }
+    const int xi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int yi = blockIdx.y * blockDim.y + threadIdx.y;
+    if (xi >= p.W || yi >= p.H) return;
+    const unsigned long long n = (unsigned long long)xi + (unsigned long long)yi * p.P;
+    const uint16_t lk = link_at(p, n);
+    if (!(lk & LINK_FLUID)) return;
+    CT<PREC> f[9];
+    nsol_even_gather<PREC, L>(f, n, xi, yi, lk, p);
+    const bool fast = lk == LINK_FLUID;
     if (is_outlet_row(xi, yi, p)) outlet_fill<PREC>(f, jy_prev_at(p, yi), p);
     const auto m = collide<PREC>(f, p);
     if (fast) {

@@ -19,6 +19,8 @@ cudaError_t launch_npol(int prec, int lay, const StepParams &p, dim3 grid, dim3 
 // debugMode's unfused step of nptl (linear = false, 2-D blocks) or lptl (linear = true, the block's
 // thread count as a 1-D block): stream, observables, collide; F64_STRICT and F32_REF (k_debug.cu).
 cudaError_t launch_debug_step(int prec, int lay, bool linear, const StepParams &p, dim3 block, cudaStream_t s);
+// Rows of a 32-wide nsol block whose even step in the collision layout stages its stores.
+constexpr int NSOL_STAGE_ROWS = 8;
 cudaError_t launch_nsol(int prec, int lay, const StepParams &p, unsigned t, dim3 grid, dim3 block, cudaStream_t s);
 
 // Set-up kernels (plbm_util.cu).
