@@ -759,12 +759,15 @@ __device__ __forceinline__ void nsol_even_collision_staged(const StepParams &p)
     }
 }
 
-// The Q60 form's staged even step in the collision layout runs a fifth resident 256-thread block.
-template <int PREC, int L> struct NsolEvenBlocks { static constexpr int value = 1; };
-template <> struct NsolEvenBlocks<F64_Q60, COLLISION> { static constexpr int value = 5; };
+// Launch bounds of the even nsol step: blocks of up to 512 threads (the host's cap for the forms
+// other than the 256-thread FP64 ones); the Q60 form's staged even step in the collision layout
+// (32 x 8 blocks) runs a fifth resident block.
+template <int PREC, int L> struct NsolEvenBounds { static constexpr int threads = 512, blocks = 1; };
+template <> struct NsolEvenBounds<F64_Q60, COLLISION> { static constexpr int threads = 256, blocks = 5; };
 
 template <int PREC, int L>
-__global__ void __launch_bounds__(256, NsolEvenBlocks<PREC, L>::value) k_nsol_even(StepParams p)
+__global__ void __launch_bounds__(NsolEvenBounds<PREC, L>::threads, NsolEvenBounds<PREC, L>::blocks)
+    k_nsol_even(StepParams p)
 {
     if constexpr (L == COLLISION) {
         if (blockDim.x == 32 && blockDim.y <= NSOL_STAGE_ROWS) {   // uniform over the grid
