@@ -276,6 +276,38 @@ def test_set_equilibrium_ignores_solid_entries(plbm, precision):
         assert np.array_equal(out[0][k], out[1][k]), k
 
 
+@pytest.mark.parametrize("fui", [60, 10])
+def test_result_readers_agree_after_host_written_steps(plbm, fui):
+    """The step loop's result steps write the observables straight into the mapped host arrays
+    (fui = 60: the last step; fui = 10: frame graphs too), so the device copies are then older:
+    mass_momentum must still sum the newest results, sync_results must leave the host arrays as
+    they are, and after device-resident steps both must follow those."""
+    w, h = 70, 33
+    mask = plbm.porous_disks(w, h, 3, 0.8)
+    fluid = mask.reshape(-1) == 0
+    props = plbm.Properties("nptl", "stream", False, 64, 60, fui, "Hagen-Poiseuille", h, w, 0.0, 0.0,
+                            1.03, 0.0, 0.0, 1.0, 0.7)
+    hd = plbm.create_handler(props, precision="f64_strict", mask=mask)
+
+    def host_sums():
+        return [float(np.sum(a[fluid])) for a in (hd.get_densities(), hd.get_x_velocities(), hd.get_y_velocities())]
+
+    hd.start()
+    hd.block_until_finished()
+    before = [hd.get_densities().copy(), hd.get_x_velocities().copy(), hd.get_y_velocities().copy()]
+    assert abs(before[1][fluid]).max() > 0                        # the run produced results
+    assert np.allclose(hd.mass_momentum(), host_sums(), rtol=1e-12, atol=1e-12)
+    hd.sync_results()
+    after = [hd.get_densities(), hd.get_x_velocities(), hd.get_y_velocities()]
+    for a, b in zip(before, after):
+        assert np.array_equal(a, b)
+    hd.run_steps(7)
+    hd.sync_results()
+    assert not np.array_equal(before[0], hd.get_densities())
+    assert np.allclose(hd.mass_momentum(), host_sums(), rtol=1e-12, atol=1e-12)
+    hd.close()
+
+
 @pytest.mark.parametrize("precision", ["f64_strict", "f64_q60"])
 def test_set_equilibrium_of_rest_state_is_the_rest_start(plbm, precision):
     """Loading rho = 1, j = 0 gives the same run as the handler's own initialisation."""
