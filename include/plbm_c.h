@@ -307,6 +307,13 @@ int plbm_set_equilibrium(plbm_handler *h, const double *rho, const double *jx, c
 int plbm_nn_conv_fwd(const void *x, const void *w, const float *bias, void *y, int N, int H, int W, int Cin, int Cout,
                      int relu, void *stream);
 int plbm_nn_conv_dgrad(const void *g, const void *w, void *gx, int N, int H, int W, int Cin, int Cout, void *stream);
+/* The input gradient of plbm_nn_conv_dgrad with the weights also given re-laid out,
+ * wt[ci][8 - tap][co] = w[co][tap][ci] (the tensor-core kernels read wt; other shapes read w). */
+int plbm_nn_conv_dgrad_pre(const void *g, const void *w, const void *wt, void *gx, int N, int H, int W, int Cin,
+                           int Cout, void *stream);
+/* wt = the layout above for `layers` layers in one launch: segs (device, 3 ints per layer) holds
+ * each layer's element offset in the flat w / wt buffers, Cin and Cout; max_elems bounds 9 Cin Cout. */
+int plbm_nn_flip_layers(const void *w, void *wt, const int *segs, int layers, int max_elems, void *stream);
 int plbm_nn_conv_wgrad(const void *x, const void *g, float *gw, float *gb, int N, int H, int W, int Cin, int Cout,
                        void *stream);
 int plbm_nn_relu_bwd(const void *y, void *g, long long n, void *stream);

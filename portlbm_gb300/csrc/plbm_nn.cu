@@ -354,6 +354,19 @@ __device__ __forceinline__ uint4 pack8(const float f[8])
     return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
+// Every layer's weights re-laid out for its input gradient in one launch: layer l = blockIdx.y,
+// segs[3l..3l+2] = (element offset of its weights in the flat buffers, Cin, Cout);
+// wt[off + (ci * 9 + 8 - tap) * Cout + co] = w[off + (co * 9 + tap) * Cin + ci].
+__global__ void k_flip_layers(const __nv_bfloat16 *w, __nv_bfloat16 *wt, const int *segs)
+{
+    const long long off = segs[3 * blockIdx.y];
+    const int Cin = segs[3 * blockIdx.y + 1], Cout = segs[3 * blockIdx.y + 2], total = Cout * 9 * Cin;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int co = i / (9 * Cin), r = i - co * 9 * Cin, tap = r / Cin, ci = r - tap * Cin;
+        wt[off + ((long long)ci * 9 + (8 - tap)) * Cout + co] = w[off + i];
+    }
+}
+
 // Eight bfloat16 gradients kept where y > 0 (a positive, non-NaN bfloat16), zeroed elsewhere.
 __device__ __forceinline__ uint4 relu_mask8(uint4 yv, uint4 gv)
 {
@@ -546,6 +559,24 @@ int plbm_nn_conv_fwd(const void *x, const void *w, const float *bias, void *y, i
     a.N = N; a.H = H; a.W = W; a.Cin = Cin; a.Cout = Cout; a.relu = relu;
     a.M = N * H * W; a.Ncols = Cout; a.K = 9 * Cin;
     return run_conv<FWD>(a, (cudaStream_t)stream);
+}
+
+int plbm_nn_flip_layers(const void *w, void *wt, const int *segs, int layers, int max_elems, void *stream)
+{
+    if (layers <= 0 || layers > 65535 || max_elems <= 0 || !segs) return PLBM_ERR_ARGUMENT;
+    const dim3 grid((unsigned)((max_elems + 255) / 256 < 64 ? (max_elems + 255) / 256 : 64), (unsigned)layers);
+    k_flip_layers<<<grid, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)w, (__nv_bfloat16 *)wt, segs);
+    return cudaGetLastError() == cudaSuccess ? PLBM_OK : PLBM_ERR_CUDA;
+}
+
+int plbm_nn_conv_dgrad_pre(const void *g, const void *w, const void *wt, void *gx, int N, int H, int W, int Cin,
+                           int Cout, void *stream)
+{
+    const bool tma = plbm_nn_tc_supported(H, W, Cout, Cin);
+    if (tma) return plbm_nn_tc_conv(g, wt, nullptr, gx, N, H, W, Cout, Cin, 0, (cudaStream_t)stream);
+    if (plbm_nn_tc_small_supported(H, W, Cout, Cin))
+        return plbm_nn_tc_small_conv(g, wt, nullptr, gx, N, H, W, Cout, Cin, 0, (cudaStream_t)stream);
+    return plbm_nn_conv_dgrad(g, w, gx, N, H, W, Cin, Cout, stream);
 }
 
 int plbm_nn_conv_dgrad(const void *g, const void *w, void *gx, int N, int H, int W, int Cin, int Cout, void *stream)

@@ -49,6 +49,8 @@ def _fns():
     sig = {
         "plbm_nn_conv_fwd": [vp, vp, vp, vp, i, i, i, i, i, i, vp],
         "plbm_nn_conv_dgrad": [vp, vp, vp, i, i, i, i, i, vp],
+        "plbm_nn_conv_dgrad_pre": [vp, vp, vp, vp, i, i, i, i, i, vp],
+        "plbm_nn_flip_layers": [vp, vp, vp, i, i, vp],
         "plbm_nn_conv_wgrad": [vp, vp, vp, vp, i, i, i, i, i, vp],
         "plbm_nn_relu_bwd": [vp, vp, ll, vp],
         "plbm_nn_relu_bwd_bias": [vp, vp, vp, ll, i, vp],
@@ -121,16 +123,19 @@ class ConvLayer:
     def __init__(self, cin, cout, relu, rng, params):
         self.cin, self.cout, self.relu = cin, cout, relu
         w = (rng.standard_normal((cout, 9 * cin)) * np.sqrt(2.0 / (9 * cin))).astype(np.float32)
-        self.w, self.gw, self.m0, self.v0, self.wb = params.segment((cout, 9 * cin))   # FP32 master, BF16 copy
-        self.b, self.gb, self.m1, self.v1, _ = params.segment((cout,))
+        # FP32 master, BF16 copy and the BF16 copy re-laid out for the input gradient (wbt)
+        self.w_off = params.off
+        self.w, self.gw, self.m0, self.v0, self.wb, self.wbt = params.segment((cout, 9 * cin))
+        self.b, self.gb, self.m1, self.v1, _, _ = params.segment((cout,))
         self.w.copy_(params.torch.from_numpy(w))
         self.wb.copy_(self.w.to(params.torch.bfloat16))
         self.m, self.v = [self.m0, self.m1], [self.v0, self.v1]
 
 
 class Params:
-    """Flat FP32 buffers for the weights and biases, their gradients and Adam's two moments, and a
-    BF16 copy of the weights: zeroing the gradients and the Adam update are one launch each."""
+    """Flat FP32 buffers for the weights and biases, their gradients and Adam's two moments, a BF16
+    copy of the weights and that copy re-laid out for the input gradients: zeroing the gradients,
+    the Adam update and the re-layout are one launch each."""
 
     def __init__(self, sizes, torch):
         self.torch = torch
@@ -138,12 +143,13 @@ class Params:
         f32 = dict(dtype=torch.float32, device="cuda")
         self.w, self.g, self.m, self.v = (torch.zeros(self.total, **f32) for _ in range(4))
         self.wb = torch.zeros(self.total, dtype=torch.bfloat16, device="cuda")
+        self.wbt = torch.zeros(self.total, dtype=torch.bfloat16, device="cuda")
         self.off = 0
 
     def segment(self, shape):
         n = int(np.prod(shape))
         a, self.off = self.off, self.off + -(-n // PARAM_ALIGN) * PARAM_ALIGN
-        return tuple(t[a:a + n].view(shape) for t in (self.w, self.g, self.m, self.v, self.wb))
+        return tuple(t[a:a + n].view(shape) for t in (self.w, self.g, self.m, self.v, self.wb, self.wbt))
 
 
 class NeuralOperator:
@@ -162,6 +168,9 @@ class NeuralOperator:
         self.dec = [ConvLayer(ci, co, True, rng, self.params) for ci, co in DEC]
         self.head = ConvLayer(HEAD[0], HEAD[1], False, rng, self.params)
         self.layers = self.enc + self.dec + [self.head]
+        # (weight offset, Cin, Cout) of every layer for the one-launch re-layout of the weights
+        self._segs = torch.tensor([[l.w_off, l.cin, l.cout] for l in self.layers], dtype=torch.int32, device="cuda")
+        self._max_elems = max(9 * l.cin * l.cout for l in self.layers)
         self.norm = np.array([1.0, 1.0])          # std of t_rho and of t_j over the training set
         self.step_count = 0
         self._s = None
@@ -243,12 +252,15 @@ class NeuralOperator:
         if not need_gx:
             return None
         gx = self._buf(n, h, w, layer.cin)
-        _ok(self.lib.plbm_nn_conv_dgrad(gy.data_ptr(), layer.wb.data_ptr(), gx.data_ptr(), n, h, w, layer.cin,
-                                        layer.cout, self._s))
+        _ok(self.lib.plbm_nn_conv_dgrad_pre(gy.data_ptr(), layer.wb.data_ptr(), layer.wbt.data_ptr(), gx.data_ptr(),
+                                            n, h, w, layer.cin, layer.cout, self._s))
         return gx
 
     def backward(self, gout):
         self._s = self._stream()
+        p = self.params
+        _ok(self.lib.plbm_nn_flip_layers(p.wb.data_ptr(), p.wbt.data_ptr(), self._segs.data_ptr(), len(self.layers),
+                                         self._max_elems, self._s))
         a, (n, h, w) = self.acts, self.shape
         g = self._conv_bwd(self.head, a["d0b"], a["out"], gout, n, h, w)
         gskip = {}

@@ -201,6 +201,47 @@ def test_pool_and_upsample(plbm):
     _close(_np(gu), nn_ref.pool2(x) * 4.0)
 
 
+def test_one_launch_weight_relayout_and_input_gradient(plbm):
+    """plbm_nn_flip_layers re-lays out several layers of a flat buffer at once as
+    wt[ci][8 - tap][co] = w[co][tap][ci], and plbm_nn_conv_dgrad_pre with it gives
+    plbm_nn_conv_dgrad's input gradient bit for bit (TMA-fed, thread-written and mma.sync shapes)."""
+    import torch
+    lib = _lib(plbm)
+    vp, i = ctypes.c_void_p, ctypes.c_int
+    lib.plbm_nn_flip_layers.argtypes = [vp, vp, vp, i, i, vp]
+    lib.plbm_nn_conv_dgrad_pre.argtypes = [vp, vp, vp, vp, i, i, i, i, i, vp]
+    rng = np.random.default_rng(12)
+    shapes = [(32, 64), (4, 32), (32, 3), (96, 128), (24, 40)]   # (Cin, Cout)
+    offs, off = [], 0
+    for ci, co in shapes:
+        offs.append(off)
+        off += -(-9 * ci * co // 128) * 128
+    wflat = np.zeros(off)
+    for (ci, co), o in zip(shapes, offs):
+        wflat[o:o + 9 * ci * co] = rng.standard_normal(9 * ci * co) * 0.1
+    wflat = nn_ref.bf16_round(wflat)
+    wd = _bf(wflat)
+    wt = torch.zeros_like(wd)
+    segs = torch.tensor([[o, ci, co] for (ci, co), o in zip(shapes, offs)], dtype=torch.int32, device="cuda")
+    assert lib.plbm_nn_flip_layers(wd.data_ptr(), wt.data_ptr(), segs.data_ptr(), len(shapes),
+                                   max(9 * ci * co for ci, co in shapes), None) == 0
+    torch.cuda.synchronize()
+    wtn = _np(wt)
+    for (ci, co), o in zip(shapes, offs):
+        w4 = wflat[o:o + 9 * ci * co].reshape(co, 9, ci)
+        assert np.array_equal(wtn[o:o + 9 * ci * co].reshape(ci, 9, co), w4[:, ::-1, :].transpose(2, 1, 0))
+    for (ci, co), o, (n, h, w) in zip(shapes, offs, [(2, 8, 256), (2, 16, 64), (1, 8, 256), (1, 32, 32), (2, 8, 24)]):
+        g = _bf(nn_ref.bf16_round(rng.standard_normal((n, h, w, co))))
+        a = torch.empty((n, h, w, ci), dtype=torch.bfloat16, device="cuda")
+        b = torch.empty_like(a)
+        n_el = 9 * ci * co
+        assert lib.plbm_nn_conv_dgrad(g.data_ptr(), wd[o:].data_ptr(), a.data_ptr(), n, h, w, ci, co, None) == 0
+        assert lib.plbm_nn_conv_dgrad_pre(g.data_ptr(), wd[o:].data_ptr(), wt[o:].data_ptr(), b.data_ptr(), n, h, w,
+                                          ci, co, None) == 0
+        torch.cuda.synchronize()
+        assert torch.equal(a, b), (ci, co, n_el)
+
+
 @pytest.mark.parametrize("p,c", [(4096, 32), (3000, 96), (777, 128), (500, 12)])
 def test_relu_backward_with_bias_gradient(plbm, p, c):
     """plbm_nn_relu_bwd_bias masks the gradient where the activation is not positive (bit-exact) and
