@@ -58,3 +58,17 @@ def test_clock_summary_from_nvml_samples():
     assert s["samples"] == 30 and s["sm_mhz"] == 2070.0 and s["reasons"] == ["sw_power_cap"]
     c.nvml_samples.append((t0 + 0.02, 1500.0, 2070.0, 0x8))
     assert "hw_slowdown" in c.summary((t0, t0 + 0.05))["reasons"]
+
+
+def test_batch_tile_argument_and_sampler_period():
+    """--batch-tile W,THREADS_Y,ROWS,BLOCKS[,vec] becomes Batch.set_tile's (tile_w, tile_h, blocks)
+    with the rows in tile_h's second byte and the vectorised-rows flag above; the clock sampler
+    queries every millisecond until relax() slows it after the device-timed steps."""
+    class Lib:
+        BATCH_TILE_VEC = 0x10000
+    assert bench.parse_batch_tile("32,4,2,4,vec", Lib) == (32, 4 + 256 * 2 + 0x10000, 4)
+    assert bench.parse_batch_tile("32,8,4,16", Lib) == (32, 8 + 256 * 4, 16)
+    c = bench.ClockSampler(0)
+    assert c.period_s == 0.001
+    c.relax()
+    assert c.period_s == 0.05
