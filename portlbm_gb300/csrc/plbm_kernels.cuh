@@ -759,22 +759,20 @@ __device__ __forceinline__ void nsol_even_collision_staged(const StepParams &p)
     }
 }
 
-// Launch bounds of the even nsol step: blocks of up to 512 threads (the host's cap for the forms
-// other than the 256-thread FP64 ones); the Q60 form's staged even step in the collision layout
-// (32 x 8 blocks) runs a fifth resident block.
-template <int PREC, int L> struct NsolEvenBounds { static constexpr int threads = 512, blocks = 1; };
-template <> struct NsolEvenBounds<F64_Q60, COLLISION> { static constexpr int threads = 256, blocks = 5; };
+// The staged even step as its own kernel (launched by launch_nsol for 32 x NSOL_STAGE_ROWS blocks
+// in the collision layout): 256 threads, four resident blocks (the 64-register cap an unbounded
+// kernel gets), five for the Q60 form (48 registers, measured faster).  The other nsol kernels keep
+// no launch bounds: a bound above 256 threads let the compiler take 98 registers for the stream
+// layout's even step and halved its resident blocks.
+template <int PREC>
+__global__ void __launch_bounds__(256, PREC == F64_Q60 ? 5 : 4) k_nsol_even_staged(StepParams p)
+{
+    nsol_even_collision_staged<PREC>(p);
+}
 
 template <int PREC, int L>
-__global__ void __launch_bounds__(NsolEvenBounds<PREC, L>::threads, NsolEvenBounds<PREC, L>::blocks)
-    k_nsol_even(StepParams p)
+__global__ void k_nsol_even(StepParams p)
 {
-    if constexpr (L == COLLISION) {
-        if (blockDim.x == 32 && blockDim.y <= NSOL_STAGE_ROWS) {   // uniform over the grid
-            nsol_even_collision_staged<PREC>(p);
-            return;
-        }
-    }
     const int xi = blockIdx.x * blockDim.x + threadIdx.x;
     const int yi = blockIdx.y * blockDim.y + threadIdx.y;
     if (xi >= p.W || yi >= p.H) return;
