@@ -723,10 +723,12 @@ __device__ __forceinline__ void nsol_even_collision_staged(const StepParams &p)
 {
     using T = typename Store<PREC>::T;
     constexpr int RW = 34, RH = NSOL_STAGE_ROWS + 2, E = RW * 9;   // entries per frame row
+    static_assert((RH * E) % 4 == 0, "the flags are cleared as 32-bit words");
     __shared__ T stage[RH * E];
-    __shared__ unsigned char written[RH * E];
+    __shared__ __align__(4) unsigned char written[RH * E];
     const int tid = threadIdx.y * 32 + threadIdx.x, nt = 32 * blockDim.y, rows = blockDim.y + 2;
-    for (int i = tid; i < rows * E; i += nt) written[i] = 0;
+    // whole words: at most RH * E bytes, since rows <= RH and RH * E is a multiple of four
+    for (int i = tid; i < (rows * E + 3) / 4; i += nt) reinterpret_cast<unsigned *>(written)[i] = 0u;
     __syncthreads();
     const int xi = blockIdx.x * 32 + threadIdx.x, yi = blockIdx.y * blockDim.y + threadIdx.y;
     const bool inside = xi < p.W && yi < p.H;
